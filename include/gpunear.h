@@ -1,0 +1,135 @@
+/*
+ * gpunear.h — C ABI of the GB300 search library (libgpunear.so).
+ *
+ * Plain pointers and sizes only.  Every call returns a gn_status; on failure
+ * gn_last_error() gives a message for the calling thread.  Results are always
+ * nearest-first; a distance tie is broken by the lower database row index.
+ *
+ * Host-pointer entry points (the drop-in surface) copy inputs to the device and
+ * results back inside the call.  *_device entry points take device pointers and
+ * a cudaStream_t passed as void*, and return without synchronising.
+ *
+ * Each declaration names the reference interface it replaces, as
+ * file:line within the PyNear 2.2.0 source tree.
+ */
+#ifndef GPUNEAR_H
+#define GPUNEAR_H
+
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#pragma GCC visibility push(default)
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    GN_OK = 0,
+    GN_ERR_INVALID = 1,     /* bad argument: shape, k, dtype width (maps to ValueError) */
+    GN_ERR_EMPTY = 2,       /* search on an index without data (maps to RuntimeError) */
+    GN_ERR_CUDA = 3,        /* CUDA runtime failure */
+    GN_ERR_OOM = 4,         /* device allocation failed */
+    GN_ERR_TIMEOUT = 5,     /* a bounded device-side wait gave up */
+    GN_ERR_UNSUPPORTED = 6  /* valid request outside the implemented limits */
+} gn_status;
+
+typedef enum {
+    GN_METRIC_L2 = 0,      /* Euclidean (sqrt) distance, float32 */
+    GN_METRIC_L1 = 1,      /* Manhattan distance, float32 */
+    GN_METRIC_LINF = 2,    /* Chebyshev distance, float32 */
+    GN_METRIC_HAMMING = 3  /* popcount(a ^ b) over uint8 rows, int64 */
+} gn_metric;
+
+typedef struct gn_index gn_index;
+
+/* library / device info */
+int gn_version(void);
+const char *gn_last_error(void);
+int gn_device_info(int *num_sms, int *cc_major, int *cc_minor);
+/* Kernel timing (no reference counterpart; used by the benchmark): while
+ * enabled, each search brackets its dominant kernel with CUDA events on the
+ * stream it launches on; gn_timing_last waits for the last bracket and reports
+ * its duration and the kernel's name. */
+int gn_timing_enable(int on);
+int gn_timing_last(float *ms, char *name, int name_len);
+
+/* ── exact flat index ─────────────────────────────────────────────────────
+ * Replaces the VP-tree indexes bound in pynear/src/PythonBindings.cpp:344-408
+ * (VPTreeNumpyAdapter::set / searchKNN / search1NN, :36-90, and the binary
+ * adapter VPTreeNumpyAdapterBinary, :147-176) with an exhaustive scan that
+ * returns the exact k nearest rows.  Distances are the reference's
+ * dist_l2_f_avx2 / dist_l1_f_avx2 / dist_chebyshev_f_avx2 values bit for bit
+ * (pynear/include/DistanceFunctions.hpp:304-420) and exact Hamming counts.
+ */
+int gn_flat_create(int metric, gn_index **out);
+/* data: n rows of dim floats (float metrics) or dim bytes (Hamming); copied. */
+int gn_flat_set(gn_index *ix, const void *data, int64_t n, int64_t dim);
+/* out_idx: nq*k int64; out_dist: nq*k float32 (float metrics) or int64
+ * (Hamming).  When k > n the trailing entries of each row are -1 / 0. */
+int gn_flat_search_knn(gn_index *ix, const void *queries, int64_t nq, int64_t k, int64_t *out_idx, void *out_dist);
+/* 1-NN shortcut (VPTree::search1NN, pynear/include/VPTree.hpp:169-191) */
+int gn_flat_search_1nn(gn_index *ix, const void *queries, int64_t nq, int64_t *out_idx, void *out_dist);
+int gn_flat_search_knn_device(gn_index *ix, const void *d_queries, int64_t nq, int64_t k, int64_t *d_idx,
+                              void *d_dist, void *stream);
+int gn_index_size(gn_index *ix, int64_t *n, int64_t *dim);
+int gn_index_destroy(gn_index *ix);
+
+/* ── float k-means coarse quantiser ───────────────────────────────────────
+ * Replaces kmeans_l2 (pynear/include/KMeans.hpp:25-126, bound as
+ * _pynear.kmeans_l2 at pynear/src/PythonBindings.cpp:305-329): k-means++
+ * seeding, Lloyd iterations with the assignment done as a GEMM on the device
+ * and FP64 centroid sums; stops when no label changes or after max_iter.
+ * labels: n int32; centroids: k*d float32; iters_out may be NULL.
+ */
+int gn_kmeans_l2(const float *data, int64_t n, int64_t d, int64_t k, int64_t max_iter, uint32_t seed,
+                 int32_t *labels, float *centroids, int64_t *iters_out);
+
+/* ── IVF-flat L2 index ────────────────────────────────────────────────────
+ * Replaces IVFFlatL2Index (pynear/forest.py:167-194; set :36-59, searchKNN
+ * :63-111).  Lists are a device-resident CSR (offsets, permuted rows, original
+ * ids); distances are squared L2; a query may get fewer than k results when
+ * its probed lists hold fewer than k rows (out_cnt gives the count).
+ */
+int gn_ivfl2_create(int32_t n_clusters, int32_t n_probe, gn_index **out);
+int gn_ivfl2_set(gn_index *ix, const float *data, int64_t n, int64_t d);
+/* build from given centroids and labels (no k-means), e.g. to reproduce an
+ * index built elsewhere; empty clusters are dropped as forest.py:51-53 does */
+int gn_ivfl2_set_assigned(gn_index *ix, const float *data, int64_t n, int64_t d, const float *centroids,
+                          int32_t n_centroids, const int32_t *labels);
+int gn_ivfl2_search_knn(gn_index *ix, const float *queries, int64_t nq, int64_t k, int64_t *out_idx,
+                        float *out_dist, int64_t *out_cnt);
+int gn_ivfl2_search_knn_device(gn_index *ix, const float *d_queries, int64_t nq, int64_t k, int64_t *d_idx,
+                               float *d_dist, int64_t *d_cnt, void *stream);
+int gn_ivfl2_set_n_probe(gn_index *ix, int32_t n_probe);
+int gn_ivfl2_info(gn_index *ix, int32_t *n_clusters_built, int32_t *n_probe, int64_t *n, int64_t *d);
+/* copy out the built state: centroids (n_clusters_built*d), list offsets
+ * (n_clusters_built+1, int64), original ids in list order (n, int64) */
+int gn_ivfl2_export(gn_index *ix, float *centroids, int64_t *offsets, int64_t *ids);
+
+/* ── IVF-flat binary index ────────────────────────────────────────────────
+ * Replaces IVFFlatBinaryIndex (pynear/include/BinaryIVF.hpp:34-227, bound at
+ * pynear/src/PythonBindings.cpp:454-466): binary k-means++ and majority-vote
+ * Lloyd iterations reproduce the reference's centroids exactly (same mt19937
+ * stream, same integer arithmetic); the search returns the lexicographic
+ * (distance, index) top-k of the probed lists.
+ */
+int gn_ivfbin_create(int32_t nlist, int32_t nprobe, int32_t max_iter, uint32_t seed, gn_index **out);
+int gn_ivfbin_set(gn_index *ix, const uint8_t *data, int64_t n, int64_t nbytes);
+int gn_ivfbin_search_knn(gn_index *ix, const uint8_t *queries, int64_t nq, int64_t k, int64_t *out_idx,
+                         int64_t *out_dist, int64_t *out_cnt);
+int gn_ivfbin_get_params(gn_index *ix, int32_t *nlist, int32_t *nprobe);
+int gn_ivfbin_set_nprobe(gn_index *ix, int32_t nprobe);
+/* copy out centroids (k*nbytes) and labels (n); k_out gets min(nlist, n) */
+int gn_ivfbin_export(gn_index *ix, uint8_t *centroids, int32_t *labels, int32_t *k_out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#if defined(__GNUC__)
+#pragma GCC visibility pop
+#endif
+
+#endif /* GPUNEAR_H */

@@ -1,0 +1,363 @@
+// flat_scan.cu — exact exhaustive k-NN scans (Hamming and float metrics).
+//
+// Work decomposition: the query set is cut into groups of WARPS*QW queries and
+// the database into n_slices row slices; one CTA handles one (slice, group)
+// unit.  Units are numbered slice-major so that the CTAs resident at the same
+// time read the same slice and share it through L2.  Each warp owns QW queries;
+// lane l scores row base+l against all of them (the row stays in registers,
+// query words come from shared memory as broadcasts), then offers the keys to
+// the warp's register top-k lists.  Each (query, slice) writes its sorted k
+// keys to a partial buffer; flat_merge_kernel reduces the slices.
+//
+// Reference semantics (pynear/include/VPTree.hpp:143-191): exact k nearest rows
+// per query; here ties go to the lower row index.
+#include "distance.cuh"
+#include "flat_scan.cuh"
+#include "timing.cuh"
+#include "topk.cuh"
+
+namespace gn {
+
+// ── Hamming scan ───────────────────────────────────────────────────────────
+// db: n rows of w4 uint4 words.  q: nq rows, same layout.
+template <int QW, int R>
+__global__ void __launch_bounds__(128) hamming_scan_kernel(const uint4 *__restrict__ db, int64_t n, int w4,
+                                                           const uint4 *__restrict__ q, int64_t nq, int k,
+                                                           int n_slices, int64_t slice_rows, int n_groups,
+                                                           uint64_t *__restrict__ part) {
+    extern __shared__ uint4 sq[];  // [WARPS*QW][w4]
+    const int warps = blockDim.x >> 5;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int unit = blockIdx.x;
+    const int slice = unit / n_groups, group = unit % n_groups;
+    const int64_t q0 = (int64_t)group * warps * QW;
+
+    for (int i = threadIdx.x; i < warps * QW * w4; i += blockDim.x) {
+        int64_t qi = q0 + i / w4;
+        sq[i] = (qi < nq) ? q[qi * w4 + (i % w4)] : make_uint4(0, 0, 0, 0);
+    }
+    __syncthreads();
+
+    const int64_t r0 = (int64_t)slice * slice_rows;
+    const int64_t r1 = min(n, r0 + slice_rows);
+    const uint4 *myq = sq + warp * QW * w4;
+
+    WarpTopK<R> lists[QW];
+    uint64_t thr[QW];
+#pragma unroll
+    for (int j = 0; j < QW; ++j) { lists[j].init(); thr[j] = KEY_EMPTY; }
+
+    for (int64_t base = r0; base < r1; base += 32) {
+        const int64_t row = base + lane;
+        const bool valid = row < r1;
+        uint32_t dist[QW];
+#pragma unroll
+        for (int j = 0; j < QW; ++j) dist[j] = 0;
+        const uint4 *rp = db + (valid ? row : r0) * w4;
+#pragma unroll 4
+        for (int c = 0; c < w4; ++c) {
+            uint4 x = ldg_nc_u4(rp + c);
+#pragma unroll
+            for (int j = 0; j < QW; ++j) dist[j] += popc4(x, myq[j * w4 + c]);
+        }
+#pragma unroll
+        for (int j = 0; j < QW; ++j) {
+            uint64_t key = valid ? make_key(dist[j], (uint32_t)row) : KEY_EMPTY;
+            lists[j].offer(key, thr[j], k);
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < QW; ++j) {
+        int64_t qi = q0 + warp * QW + j;
+        if (qi < nq) lists[j].store(part + ((size_t)qi * n_slices + slice) * k, k);
+    }
+}
+
+// ── float scan (L2 / L1 / Linf in the reference's arithmetic order) ───────
+// db: n rows of dp floats (dp % 4 == 0, zero padded past d).
+template <int METRIC, int QW, int R>
+__global__ void __launch_bounds__(128) float_scan_kernel(const float *__restrict__ db, int64_t n, int d, int dp,
+                                                         const float *__restrict__ q, int64_t nq, int k,
+                                                         int n_slices, int64_t slice_rows, int n_groups,
+                                                         uint64_t *__restrict__ part) {
+    extern __shared__ float4 sqf[];  // [WARPS*QW][dp/4]
+    const int warps = blockDim.x >> 5;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int unit = blockIdx.x;
+    const int slice = unit / n_groups, group = unit % n_groups;
+    const int64_t q0 = (int64_t)group * warps * QW;
+    const int dp4 = dp >> 2;
+
+    const float4 *q4 = reinterpret_cast<const float4 *>(q);
+    for (int i = threadIdx.x; i < warps * QW * dp4; i += blockDim.x) {
+        int64_t qi = q0 + i / dp4;
+        sqf[i] = (qi < nq) ? q4[qi * dp4 + (i % dp4)] : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    __syncthreads();
+
+    const int64_t r0 = (int64_t)slice * slice_rows;
+    const int64_t r1 = min(n, r0 + slice_rows);
+    const float4 *myq = sqf + warp * QW * dp4;
+    const int nb = d >> 3, rem = d & 7;
+
+    WarpTopK<R> lists[QW];
+    uint64_t thr[QW];
+#pragma unroll
+    for (int j = 0; j < QW; ++j) { lists[j].init(); thr[j] = KEY_EMPTY; }
+
+    const float4 zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int64_t base = r0; base < r1; base += 32) {
+        const int64_t row = base + lane;
+        const bool valid = row < r1;
+        const float4 *rp = reinterpret_cast<const float4 *>(db) + (valid ? row : r0) * dp4;
+        FAcc<METRIC> acc[QW];
+#pragma unroll
+        for (int j = 0; j < QW; ++j) acc[j].zero();
+#pragma unroll 2
+        for (int c = 0; c < nb; ++c) {
+            float4 x0 = ldg_nc_f4(rp + 2 * c), x1 = ldg_nc_f4(rp + 2 * c + 1);
+#pragma unroll
+            for (int j = 0; j < QW; ++j) acc[j].block8(myq[j * dp4 + 2 * c], myq[j * dp4 + 2 * c + 1], x0, x1);
+        }
+        float4 x0 = zero4, x1 = zero4;
+        if (rem > 0) x0 = ldg_nc_f4(rp + 2 * nb);
+        if (rem > 4) x1 = ldg_nc_f4(rp + 2 * nb + 1);
+#pragma unroll
+        for (int j = 0; j < QW; ++j) {
+            float4 qa = zero4, qb = zero4;
+            if (rem > 0) qa = myq[j * dp4 + 2 * nb];
+            if (rem > 4) qb = myq[j * dp4 + 2 * nb + 1];
+            float dist = acc[j].finish(rem, qa, qb, x0, x1);
+            uint64_t key = valid ? make_key(__float_as_uint(dist), (uint32_t)row) : KEY_EMPTY;
+            lists[j].offer(key, thr[j], k);
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < QW; ++j) {
+        int64_t qi = q0 + warp * QW + j;
+        if (qi < nq) lists[j].store(part + ((size_t)qi * n_slices + slice) * k, k);
+    }
+}
+
+// ── merge of per-slice partial lists → final output ───────────────────────
+// One warp per query.  Output: idx (int64, -1 for empty), dist as float32
+// (float metrics) or int64 (Hamming).
+template <int R>
+__global__ void flat_merge_kernel(const uint64_t *__restrict__ part, int n_slices, int k, int64_t nq, int is_hamming,
+                                  int64_t *__restrict__ out_idx, void *__restrict__ out_dist) {
+    const int lane = threadIdx.x & 31;
+    const int64_t qi = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (qi >= nq) return;
+    WarpTopK<R> L;
+    L.init();
+    uint64_t thr = KEY_EMPTY;
+    const uint64_t *p = part + (size_t)qi * n_slices * k;
+    for (int s = 0; s < n_slices; ++s) {
+        for (int j0 = 0; j0 < k; j0 += 32) {
+            int j = j0 + lane;
+            uint64_t key = (j < k) ? p[(size_t)s * k + j] : KEY_EMPTY;
+            // partial lists are sorted: once the smallest unseen key of this
+            // chunk is above the threshold the rest of the list is too
+            if (__all_sync(0xffffffffu, key >= thr)) break;
+            L.offer(key, thr, k);
+        }
+    }
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+        int pos = r * 32 + lane;
+        if (pos < k) {
+            uint64_t key = L.v[r];
+            bool e = key == KEY_EMPTY;
+            out_idx[qi * k + pos] = e ? -1 : (int64_t)key_idx(key);
+            if (is_hamming) reinterpret_cast<int64_t *>(out_dist)[qi * k + pos] = e ? 0 : (int64_t)key_dist(key);
+            else reinterpret_cast<float *>(out_dist)[qi * k + pos] = e ? 0.f : __uint_as_float(key_dist(key));
+        }
+    }
+}
+
+// ── large-k path: materialised keys + radix select + bitonic sort ────────
+template <int METRIC>
+__global__ void flat_keys_kernel(const void *__restrict__ db, int64_t n, int d, int stride4,
+                                 const void *__restrict__ q, int64_t q_begin, int64_t qc,
+                                 uint64_t *__restrict__ keys) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t qq = t / n, row = t % n;
+    if (qq >= qc) return;
+    const int64_t qi = q_begin + qq;
+    uint32_t bits;
+    if (METRIC == M_HAMMING) {
+        bits = hdist(reinterpret_cast<const uint4 *>(q) + qi * stride4, reinterpret_cast<const uint4 *>(db) + row * stride4,
+                     stride4);
+    } else {
+        bits = __float_as_uint(fdist<METRIC>(reinterpret_cast<const float *>(q) + qi * stride4 * 4,
+                                             reinterpret_cast<const float *>(db) + row * stride4 * 4, d));
+    }
+    keys[qq * n + row] = make_key(bits, (uint32_t)row);
+}
+
+// One CTA per query: exact k-th smallest key by MSD radix select (8-bit
+// digits), gather the k keys at or below it, bitonic-sort them in place.
+__global__ void __launch_bounds__(1024) radix_select_sort_kernel(const uint64_t *__restrict__ keys, int64_t n,
+                                                                 int64_t k, int64_t pow2,
+                                                                 uint64_t *__restrict__ sorted) {
+    __shared__ uint32_t hist[256];
+    __shared__ uint64_t s_prefix, s_mask;
+    __shared__ int64_t s_krem;
+    __shared__ unsigned long long s_count;
+    const uint64_t *kq = keys + (int64_t)blockIdx.x * n;
+    uint64_t *out = sorted + (int64_t)blockIdx.x * pow2;
+    if (threadIdx.x == 0) { s_prefix = 0; s_mask = 0; s_krem = k; }
+    __syncthreads();
+    for (int shift = 56; shift >= 0; shift -= 8) {
+        for (int i = threadIdx.x; i < 256; i += blockDim.x) hist[i] = 0;
+        __syncthreads();
+        const uint64_t prefix = s_prefix, mask = s_mask;
+        for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
+            uint64_t v = kq[i];
+            if ((v & mask) == prefix) atomicAdd(&hist[(v >> shift) & 0xff], 1u);
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            int64_t krem = s_krem, acc = 0;
+            int dgt = 0;
+            for (; dgt < 256; ++dgt) {
+                if (acc + (int64_t)hist[dgt] >= krem) break;
+                acc += hist[dgt];
+            }
+            s_krem = krem - acc;
+            s_prefix = prefix | ((uint64_t)dgt << shift);
+            s_mask = mask | (0xffull << shift);
+        }
+        __syncthreads();
+    }
+    const uint64_t kth = s_prefix;  // exact k-th smallest key (keys are unique)
+    if (threadIdx.x == 0) s_count = 0;
+    __syncthreads();
+    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
+        uint64_t v = kq[i];
+        if (v <= kth) out[atomicAdd(&s_count, 1ull)] = v;
+    }
+    for (int64_t i = k + threadIdx.x; i < pow2; i += blockDim.x) out[i] = KEY_EMPTY;
+    __syncthreads();
+    for (int64_t size = 2; size <= pow2; size <<= 1) {
+        for (int64_t stride = size >> 1; stride > 0; stride >>= 1) {
+            for (int64_t i = threadIdx.x; i < pow2 / 2; i += blockDim.x) {
+                int64_t lo = (i / stride) * stride * 2 + (i % stride);
+                int64_t hi = lo + stride;
+                bool up = ((lo & size) == 0);
+                uint64_t a = out[lo], b = out[hi];
+                if ((a > b) == up) { out[lo] = b; out[hi] = a; }
+            }
+            __syncthreads();
+        }
+    }
+}
+
+__global__ void keys_to_output_kernel(const uint64_t *__restrict__ sorted, int64_t pow2, int64_t qc, int64_t k,
+                                      int64_t q_begin, int is_hamming, int64_t *__restrict__ out_idx,
+                                      void *__restrict__ out_dist) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= qc * k) return;
+    const int64_t qq = t / k, j = t % k;
+    uint64_t key = sorted[qq * pow2 + j];
+    bool e = key == KEY_EMPTY;
+    const int64_t o = (q_begin + qq) * k + j;
+    out_idx[o] = e ? -1 : (int64_t)key_idx(key);
+    if (is_hamming) reinterpret_cast<int64_t *>(out_dist)[o] = e ? 0 : (int64_t)key_dist(key);
+    else reinterpret_cast<float *>(out_dist)[o] = e ? 0.f : __uint_as_float(key_dist(key));
+}
+
+// ── host-side launchers ───────────────────────────────────────────────────
+template <int R>
+static void launch_scan(const FlatScanArgs &a, int n_groups, int threads, size_t smem, uint64_t *part,
+                        cudaStream_t st) {
+    const int units = n_groups * a.n_slices;
+    timing_begin(st, a.metric == M_HAMMING ? "hamming_scan_kernel" : "float_scan_kernel");
+    if (a.metric == M_HAMMING) {
+        auto kern = hamming_scan_kernel<8, R>;
+        if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        kern<<<units, threads, smem, st>>>(reinterpret_cast<const uint4 *>(a.db), a.n, a.stride4,
+                                           reinterpret_cast<const uint4 *>(a.q), a.nq, a.k, a.n_slices, a.slice_rows,
+                                           n_groups, part);
+    } else {
+#define GN_FLOAT_SCAN(M)                                                                                          \
+    do {                                                                                                          \
+        auto kern = float_scan_kernel<M, 4, R>;                                                                   \
+        if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); \
+        kern<<<units, threads, smem, st>>>(reinterpret_cast<const float *>(a.db), a.n, a.d, a.stride4 * 4,        \
+                                           reinterpret_cast<const float *>(a.q), a.nq, a.k, a.n_slices,           \
+                                           a.slice_rows, n_groups, part);                                         \
+    } while (0)
+        if (a.metric == M_L2) GN_FLOAT_SCAN(M_L2);
+        else if (a.metric == M_L1) GN_FLOAT_SCAN(M_L1);
+        else GN_FLOAT_SCAN(M_LINF);
+#undef GN_FLOAT_SCAN
+    }
+    timing_end(st);
+    const int qpb = 4;  // queries (warps) per merge block
+    flat_merge_kernel<R><<<(unsigned)ceil_div(a.nq, qpb), qpb * 32, 0, st>>>(
+        part, a.n_slices, a.k, a.nq, a.metric == M_HAMMING, a.out_idx, a.out_dist);
+}
+
+void flat_plan(FlatScanArgs &a) {
+    const DevInfo &di = dev_info();
+    const int qw = (a.metric == M_HAMMING) ? 8 : 4;
+    const size_t per_warp = (size_t)qw * a.stride4 * 16;
+    int warps = 4;
+    while (warps > 1 && per_warp * warps > 200 * 1024) warps >>= 1;
+    a.warps = warps;
+    a.qw = qw;
+    const int64_t n_groups = ceil_div(a.nq, (int64_t)warps * qw);
+    // aim for ~16 CTAs per SM over the launch, slices of at least 512 rows
+    const int64_t target = 16LL * di.num_sms;
+    int64_t slices = std::max<int64_t>(1, ceil_div(target, n_groups));
+    slices = std::min<int64_t>(slices, std::max<int64_t>(1, a.n / 512));
+    a.slice_rows = round_up(ceil_div(a.n, slices), 32);
+    a.n_slices = (int)ceil_div(a.n, a.slice_rows);
+    a.n_groups = (int)n_groups;
+}
+
+size_t flat_part_bytes(const FlatScanArgs &a) { return (size_t)a.nq * a.n_slices * a.k * sizeof(uint64_t); }
+
+int flat_smem_ok(const FlatScanArgs &a) {
+    const size_t smem = (size_t)a.warps * a.qw * a.stride4 * 16;
+    return smem <= (size_t)dev_info().max_smem_optin;
+}
+
+// Launch the warp-select path (k <= 256).  part: flat_part_bytes(a) scratch.
+void flat_launch(const FlatScanArgs &a, uint64_t *part, cudaStream_t st) {
+    const int threads = a.warps * 32;
+    const size_t smem = (size_t)a.warps * a.qw * a.stride4 * 16;
+    if (a.k <= 32) launch_scan<1>(a, a.n_groups, threads, smem, part, st);
+    else if (a.k <= 64) launch_scan<2>(a, a.n_groups, threads, smem, part, st);
+    else if (a.k <= 128) launch_scan<4>(a, a.n_groups, threads, smem, part, st);
+    else launch_scan<8>(a, a.n_groups, threads, smem, part, st);
+}
+
+int64_t next_pow2(int64_t v) {
+    int64_t p = 1;
+    while (p < v) p <<= 1;
+    return p;
+}
+
+// Large-k path for one chunk of queries [q_begin, q_begin + qc).
+// keys: qc*n scratch; sorted: qc*next_pow2(k) scratch.
+void flat_large_k_launch(const FlatScanArgs &a, int64_t q_begin, int64_t qc, uint64_t *keys, uint64_t *sorted,
+                         cudaStream_t st) {
+    const int64_t total = qc * a.n;
+    const unsigned blocks = (unsigned)ceil_div(total, 256);
+    switch (a.metric) {
+    case M_HAMMING: flat_keys_kernel<M_HAMMING><<<blocks, 256, 0, st>>>(a.db, a.n, a.d, a.stride4, a.q, q_begin, qc, keys); break;
+    case M_L2: flat_keys_kernel<M_L2><<<blocks, 256, 0, st>>>(a.db, a.n, a.d, a.stride4, a.q, q_begin, qc, keys); break;
+    case M_L1: flat_keys_kernel<M_L1><<<blocks, 256, 0, st>>>(a.db, a.n, a.d, a.stride4, a.q, q_begin, qc, keys); break;
+    default: flat_keys_kernel<M_LINF><<<blocks, 256, 0, st>>>(a.db, a.n, a.d, a.stride4, a.q, q_begin, qc, keys); break;
+    }
+    const int64_t kk = std::min<int64_t>(a.k, a.n);
+    const int64_t p2 = next_pow2(a.k);
+    radix_select_sort_kernel<<<(unsigned)qc, 1024, 0, st>>>(keys, a.n, kk, p2, sorted);
+    keys_to_output_kernel<<<(unsigned)ceil_div(qc * a.k, 256), 256, 0, st>>>(sorted, p2, qc, a.k, q_begin,
+                                                                              a.metric == M_HAMMING, a.out_idx,
+                                                                              a.out_dist);
+}
+
+}  // namespace gn

@@ -1,0 +1,69 @@
+// index.cuh — host-side index object shared by the C ABI translation units.
+#pragma once
+
+#include <mutex>
+#include <vector>
+
+#include "common.cuh"
+
+namespace gn {
+
+// Growable device allocation owned by an index (freed in the destructor).
+struct DBuf {
+    void *p = nullptr;
+    size_t cap = 0;
+    int ensure(size_t bytes);
+    void release();
+    template <typename T>
+    T *as() const { return reinterpret_cast<T *>(p); }
+    ~DBuf() { release(); }
+    DBuf() = default;
+    DBuf(const DBuf &) = delete;
+    DBuf &operator=(const DBuf &) = delete;
+};
+
+// Pinned host staging buffer.
+struct HBuf {
+    void *p = nullptr;
+    size_t cap = 0;
+    int ensure(size_t bytes);
+    void release();
+    ~HBuf() { release(); }
+    HBuf() = default;
+    HBuf(const HBuf &) = delete;
+    HBuf &operator=(const HBuf &) = delete;
+};
+
+enum IndexKind { K_FLAT = 1, K_IVFL2 = 2, K_IVFBIN = 3 };
+
+struct IvfL2State;
+struct IvfBinState;
+
+}  // namespace gn
+
+struct gn_index {
+    int kind = 0;
+    int metric = 0;
+    int64_t n = 0;        // rows
+    int64_t dim = 0;      // floats (float metrics) or bytes (binary)
+    int stride4 = 0;      // row stride in 16-byte units
+    gn::DBuf data;        // n * stride4 * 16 bytes, zero padded
+    cudaStream_t stream = nullptr;
+    std::mutex mu;
+    // per-call scratch (reused across calls)
+    gn::DBuf q, part, out_idx, out_dist, keys, sorted;
+    // kind-specific state
+    gn::IvfL2State *ivfl2 = nullptr;
+    gn::IvfBinState *ivfbin = nullptr;
+    ~gn_index();
+};
+
+namespace gn {
+
+int make_stream(gn_index *ix);
+// Copy n rows of `dim` elements of `elem` bytes from host into a device buffer
+// with row stride stride4*16 bytes, zero padding the tail of each row.
+int upload_rows(DBuf &dst, const void *src, int64_t n, int64_t row_bytes, int stride4, cudaStream_t st,
+                bool src_on_device = false);
+
+}  // namespace gn

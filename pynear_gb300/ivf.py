@@ -1,0 +1,210 @@
+"""IVF-flat indexes and the k-means coarse quantiser on the GPU.
+
+``IVFFlatL2Index`` mirrors pynear.IVFFlatL2Index (pynear/forest.py:167-194):
+constructor ``(n_clusters=100, n_probe=10)``, ``set``, ``searchKNN``,
+``search1NN``, properties ``n_clusters`` (clusters actually built, empty ones
+dropped) and ``n_probe``; distances are squared L2, nearest-first; a 1-D query
+is treated as one row; a query may get fewer than k results.
+
+``IVFFlatBinaryIndex`` mirrors the reference binding
+(pynear/src/PythonBindings.cpp:454-466): ``(nlist=256, nprobe=8, max_iter=20,
+seed=42)``, ``set``, ``searchKNN``, ``nlist()``, ``nprobe()``,
+``set_nprobe()``; Hamming distances as int64, ascending.
+
+``kmeans_l2(data, k, max_iter=100, seed=42)`` mirrors _pynear.kmeans_l2
+(pynear/src/PythonBindings.cpp:305-329) and returns (labels int32, centroids
+float32).
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from . import _lib
+
+
+def _f32_2d(a, what: str) -> np.ndarray:
+    arr = np.ascontiguousarray(np.asarray(a, dtype=np.float32))
+    if arr.ndim != 2:
+        raise ValueError(f"{what} must be a 2-D array of shape (N, D)")
+    return arr
+
+
+def kmeans_l2(data, k: int, max_iter: int = 100, seed: int = 42):
+    """Lloyd k-means with k-means++ seeding on the GPU -> (labels, centroids)."""
+    arr = np.ascontiguousarray(np.asarray(data), dtype=np.float32)
+    if arr.ndim != 2:
+        raise RuntimeError("kmeans_l2: data must be a 2D float32 array (N, D)")
+    n, d = arr.shape
+    if k <= 0 or k > n:
+        raise RuntimeError("kmeans_l2: k must be between 1 and N")
+    labels = np.empty(n, np.int32)
+    cent = np.empty((k, d), np.float32)
+    iters = np.zeros(1, np.int64)
+    _lib.call("gn_kmeans_l2", _lib.ptr(arr), n, d, int(k), int(max_iter), int(seed) & 0xffffffff,
+              _lib.ptr(labels), _lib.ptr(cent), _lib.ptr(iters))
+    return labels, cent
+
+
+def _rows_to_lists(idx: np.ndarray, dist: np.ndarray, cnt: np.ndarray, as_int: bool):
+    out_i, out_d = [], []
+    for i in range(idx.shape[0]):
+        c = int(cnt[i])
+        out_i.append(idx[i, :c].tolist())
+        out_d.append(dist[i, :c].tolist())
+    return out_i, out_d
+
+
+class IVFFlatL2Index:
+    """GPU IVF-flat over squared L2 (drop-in for pynear.IVFFlatL2Index)."""
+
+    def __init__(self, n_clusters: int = 100, n_probe: int = 10):
+        self._n_clusters_req = int(n_clusters)
+        self._n_probe = min(int(n_probe), int(n_clusters))
+        self._h = _lib.Handle("gn_ivfl2_create", self._n_clusters_req, self._n_probe)
+        self._built = False
+        self._state = None  # host copy for pickling: (data, centroids, labels)
+
+    def set(self, data) -> None:
+        arr = _f32_2d(data, "data")
+        n, d = arr.shape
+        _lib.call("gn_ivfl2_set", self._h.h, _lib.ptr(arr), n, d)
+        self._built = n > 0
+        self._state = None
+        self._data = arr
+
+    def set_assigned(self, data, centroids, labels) -> None:
+        """Build the lists from given centroids and labels (no k-means)."""
+        arr = _f32_2d(data, "data")
+        cent = _f32_2d(centroids, "centroids")
+        lab = np.ascontiguousarray(labels, dtype=np.int32)
+        _lib.call("gn_ivfl2_set_assigned", self._h.h, _lib.ptr(arr), arr.shape[0], arr.shape[1], _lib.ptr(cent),
+                  cent.shape[0], _lib.ptr(lab))
+        self._built = arr.shape[0] > 0
+        self._data = arr
+
+    def search_knn_arrays(self, queries, k: int):
+        """(idx (nq,k) int64, dist (nq,k) float32, count (nq,) int64), nearest-first."""
+        q = np.asarray(queries, dtype=np.float32)
+        if q.ndim == 1:
+            q = q[np.newaxis]
+        q = np.ascontiguousarray(q)
+        if not self._built:
+            raise RuntimeError("Index is empty — call set() first")
+        k = int(k)
+        nq = q.shape[0]
+        idx = np.empty((nq, k), np.int64)
+        dist = np.empty((nq, k), np.float32)
+        cnt = np.empty(nq, np.int64)
+        if nq:
+            _lib.call("gn_ivfl2_search_knn", self._h.h, _lib.ptr(q), nq, k, _lib.ptr(idx), _lib.ptr(dist),
+                      _lib.ptr(cnt))
+        return idx, dist, cnt
+
+    def searchKNN(self, queries, k: int):
+        idx, dist, cnt = self.search_knn_arrays(queries, k)
+        return _rows_to_lists(idx, dist, cnt, False)
+
+    def search1NN(self, queries):
+        return self.searchKNN(queries, 1)
+
+    @property
+    def n_clusters(self) -> int:
+        if not self._built:
+            return 0
+        nc = np.zeros(1, np.int32)
+        _lib.call("gn_ivfl2_info", self._h.h, _lib.ptr(nc), None, None, None)
+        return int(nc[0])
+
+    @property
+    def n_probe(self) -> int:
+        return self._n_probe
+
+    @n_probe.setter
+    def n_probe(self, value: int) -> None:
+        self._n_probe = int(value)
+        _lib.call("gn_ivfl2_set_n_probe", self._h.h, self._n_probe)
+
+    def export(self):
+        """(centroids (C,D), offsets (C+1,), ids in list order (N,)) of the built CSR lists."""
+        nc = self.n_clusters
+        d = self._data.shape[1]
+        cent = np.empty((nc, d), np.float32)
+        offs = np.empty(nc + 1, np.int64)
+        ids = np.empty(self._data.shape[0], np.int64)
+        _lib.call("gn_ivfl2_export", self._h.h, _lib.ptr(cent), _lib.ptr(offs), _lib.ptr(ids))
+        return cent, offs, ids
+
+    def __getstate__(self):
+        st = {"n_clusters": self._n_clusters_req, "n_probe": self._n_probe, "built": self._built}
+        if self._built:
+            cent, offs, ids = self.export()
+            labels = np.empty(self._data.shape[0], np.int32)
+            for c in range(len(offs) - 1):
+                labels[ids[offs[c]:offs[c + 1]]] = c
+            st.update(data=self._data, centroids=cent, labels=labels)
+        return st
+
+    def __setstate__(self, st):
+        self.__init__(st["n_clusters"], st["n_probe"])
+        if st["built"]:
+            self.set_assigned(st["data"], st["centroids"], st["labels"])
+
+
+class IVFFlatBinaryIndex:
+    """GPU IVF-flat over Hamming distance (drop-in for pynear.IVFFlatBinaryIndex)."""
+
+    def __init__(self, nlist: int = 256, nprobe: int = 8, max_iter: int = 20, seed: int = 42):
+        self._args = (int(nlist), int(nprobe), int(max_iter), int(seed) & 0xffffffff)
+        self._h = _lib.Handle("gn_ivfbin_create", *self._args)
+        self._n = 0
+        self._nbytes = 0
+
+    def set(self, vectors) -> None:
+        arr = np.ascontiguousarray(vectors)
+        if arr.ndim != 2:
+            raise ValueError("invalid data shape: binary indexes must be 2D")
+        if arr.dtype != np.uint8:
+            arr = arr.astype(np.uint8)
+        n, nb = arr.shape
+        _lib.call("gn_ivfbin_set", self._h.h, _lib.ptr(arr), n, nb)
+        self._n, self._nbytes = n, nb
+
+    def search_knn_arrays(self, queries, k: int):
+        q = np.ascontiguousarray(queries)
+        if q.ndim != 2:
+            raise ValueError("invalid data shape: binary indexes must be 2D")
+        if q.dtype != np.uint8:
+            q = q.astype(np.uint8)
+        k = int(k)
+        nq = q.shape[0]
+        idx = np.empty((nq, k), np.int64)
+        dist = np.empty((nq, k), np.int64)
+        cnt = np.zeros(nq, np.int64)
+        if nq and self._n:
+            _lib.call("gn_ivfbin_search_knn", self._h.h, _lib.ptr(q), nq, k, _lib.ptr(idx), _lib.ptr(dist),
+                      _lib.ptr(cnt))
+        return idx, dist, cnt
+
+    def searchKNN(self, vectors, k: int):
+        idx, dist, cnt = self.search_knn_arrays(vectors, k)
+        return _rows_to_lists(idx, dist, cnt, True)
+
+    def nlist(self) -> int:
+        return self._args[0]
+
+    def nprobe(self) -> int:
+        a = np.zeros(2, np.int32)
+        _lib.call("gn_ivfbin_get_params", self._h.h, _lib.ptr(a[:1]), _lib.ptr(a[1:]))
+        return int(a[1])
+
+    def set_nprobe(self, nprobe: int) -> None:
+        _lib.call("gn_ivfbin_set_nprobe", self._h.h, int(nprobe))
+
+    def export(self):
+        """(centroids (k, nbytes) uint8, labels (n,) int32) of the built index."""
+        kk = min(self._args[0], self._n)
+        cent = np.empty((kk, self._nbytes), np.uint8)
+        labels = np.empty(self._n, np.int32)
+        kout = np.zeros(1, np.int32)
+        _lib.call("gn_ivfbin_export", self._h.h, _lib.ptr(cent), _lib.ptr(labels), _lib.ptr(kout))
+        return cent[: int(kout[0])], labels

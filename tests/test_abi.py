@@ -1,0 +1,91 @@
+"""CPU-side checks of the C ABI library and the host-side API logic (no GPU)."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+from conftest import REPO
+
+
+def _declared_symbols():
+    text = open(os.path.join(REPO, "include", "gpunear.h")).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(gn_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_library_builds_and_exports_every_declared_symbol(gn):
+    from pynear_gb300 import _lib
+    lib = ctypes.CDLL(_lib.LIB_PATH)
+    names = _declared_symbols()
+    assert len(names) >= 20
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+    # the Python binding declares a signature for every exported entry point
+    assert set(names) <= set(_lib.SIGNATURES)
+
+
+def test_version_and_error_string(gn):
+    from pynear_gb300 import _lib
+    lib = _lib.load()
+    assert lib.gn_version() >= 100
+    assert isinstance(_lib.last_error(), str)
+
+
+def test_status_mapping():
+    from pynear_gb300 import _lib
+    with pytest.raises(ValueError):
+        _lib.check(_lib.GN_ERR_INVALID, "x")
+    with pytest.raises(RuntimeError):
+        _lib.check(_lib.GN_ERR_EMPTY, "x")
+    with pytest.raises(MemoryError):
+        _lib.check(_lib.GN_ERR_OOM, "x")
+    with pytest.raises(_lib.GpuNearError):
+        _lib.check(_lib.GN_ERR_TIMEOUT, "x")
+    _lib.check(_lib.GN_OK)
+
+
+def test_create_rejects_bad_metric(gn):
+    from pynear_gb300 import _lib
+    h = ctypes.c_void_p()
+    assert _lib.load().gn_flat_create(17, ctypes.byref(h)) == _lib.GN_ERR_INVALID
+    assert "metric" in _lib.last_error()
+
+
+def test_binary_wrapper_validation_matches_reference(gn):
+    # pynear/__init__.py:99-104: 2-D check first (ValueError), then uint8 (TypeError)
+    ix = gn.VPTreeBinaryIndex()
+    with pytest.raises(ValueError):
+        ix.set(np.zeros((4,), np.uint8))
+    with pytest.raises(TypeError):
+        ix.set(np.zeros((4, 8), np.float32))
+    # searching an index that was never set returns empty lists
+    assert ix.search1NN(np.zeros((1, 8), np.uint8)) == ([], [])
+
+
+def test_float_wrapper_rejects_non_2d(gn):
+    ix = gn.VPTreeL2Index()
+    with pytest.raises(RuntimeError):
+        ix.set(np.zeros((5,), np.float32))
+
+
+def test_empty_flat_index_raises(gn):
+    ix = gn.FlatL2Index()
+    with pytest.raises(RuntimeError):
+        ix.searchKNN(np.zeros((1, 4), np.float32), 1)
+
+
+def test_ivf_empty_raises(gn):
+    ix = gn.IVFFlatL2Index(n_clusters=4, n_probe=2)
+    with pytest.raises(RuntimeError):
+        ix.searchKNN(np.zeros((1, 4), np.float32), 1)
+    assert ix.n_probe == 2
+    assert ix.n_clusters == 0
+
+
+def test_kmeans_argument_checks(gn):
+    with pytest.raises(RuntimeError):
+        gn.kmeans_l2(np.zeros((5, 2), np.float32), 6)
+    with pytest.raises(RuntimeError):
+        gn.kmeans_l2(np.zeros((5,), np.float32), 2)
