@@ -93,6 +93,7 @@ int upload_rows(DBuf &dst, const void *src, int64_t n, int64_t row_bytes, int st
 }  // namespace gn
 
 gn_index::~gn_index() {
+    gn::ivf_free(this);
     if (stream) {
         cudaStreamSynchronize(stream);
         cudaStreamDestroy(stream);

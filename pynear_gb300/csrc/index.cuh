@@ -61,6 +61,7 @@ struct gn_index {
 namespace gn {
 
 int make_stream(gn_index *ix);
+void ivf_free(gn_index *ix);
 // Copy n rows of `dim` elements of `elem` bytes from host into a device buffer
 // with row stride stride4*16 bytes, zero padding the tail of each row.
 int upload_rows(DBuf &dst, const void *src, int64_t n, int64_t row_bytes, int stride4, cudaStream_t st,

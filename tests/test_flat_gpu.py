@@ -15,7 +15,7 @@ COMPAT_CLASSES = {"l2": "VPTreeL2Index", "l1": "VPTreeL1Index", "linf": "VPTreeC
 
 
 def _flat(gn, metric, db):
-    ix = getattr(gn, FLAT_CLASSES[metric])()
+    ix = getattr(gn, FLOAT_CLASSES[metric])()
     ix.set(db)
     return ix
 
