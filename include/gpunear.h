@@ -76,6 +76,26 @@ int gn_flat_search_knn_device(gn_index *ix, const void *d_queries, int64_t nq, i
 int gn_index_size(gn_index *ix, int64_t *n, int64_t *dim);
 int gn_index_destroy(gn_index *ix);
 
+/* ── exact L2 via a tensor-core shortlist ─────────────────────────────────
+ * Same contract as gn_flat_search_knn for GN_METRIC_L2 (the exact Euclidean
+ * k nearest rows, the reference's dist_l2_f_avx2 values), computed in two
+ * stages: a BF16 tcgen05 GEMM scores |x|^2 - 2 q.x with FP32 accumulation and
+ * keeps the `shortlist` best rows per query, then those are re-ranked with the
+ * reference's FP32 distance.  Exact whenever the true k nearest rows are inside
+ * the shortlist.  Shortlist: 16, 32, 40 or 64; k <= min(32, shortlist).
+ * Replaces VPTreeL2Index (pynear/src/PythonBindings.cpp:344-350) for
+ * large batches.
+ */
+int gn_tcflat_create(int32_t shortlist, gn_index **out);
+int gn_tcflat_set(gn_index *ix, const float *data, int64_t n, int64_t d);
+int gn_tcflat_search_knn(gn_index *ix, const float *queries, int64_t nq, int64_t k, int64_t *out_idx,
+                         float *out_dist);
+/* d_queries: nq rows of round_up(d, 4) floats (zero padded) on the device */
+int gn_tcflat_search_knn_device(gn_index *ix, const float *d_queries, int64_t nq, int64_t k, int64_t *d_idx,
+                                float *d_dist, void *stream);
+/* error word of the last tensor-core launch (nonzero: a bounded wait expired) */
+int gn_tc_error(gn_index *ix, int32_t *err_out);
+
 /* ── float k-means coarse quantiser ───────────────────────────────────────
  * Replaces kmeans_l2 (pynear/include/KMeans.hpp:25-126, bound as
  * _pynear.kmeans_l2 at pynear/src/PythonBindings.cpp:305-329): k-means++

@@ -4,7 +4,7 @@ The index classes keep PyNear's API (``set`` / ``searchKNN`` / ``search1NN``
 returning ``(indices, distances)``) and run every search on the GPU through
 libgpunear.so (C ABI in include/gpunear.h).
 """
-from .flat import (FlatChebyshevIndex, FlatHammingIndex, FlatL1Index, FlatL2Index, VPTreeBinaryIndex,
+from .flat import (FlatChebyshevIndex, FlatHammingIndex, FlatL1Index, FlatL2Index, FlatL2TCIndex, VPTreeBinaryIndex,
                    VPTreeChebyshevIndex, VPTreeL1Index, VPTreeL2Index, dist_chebyshev, dist_hamming, dist_l1,
                    dist_l2)
 from .ivf import IVFFlatBinaryIndex, IVFFlatL2Index, kmeans_l2
@@ -12,7 +12,7 @@ from .ivf import IVFFlatBinaryIndex, IVFFlatL2Index, kmeans_l2
 __version__ = "0.1.0"
 
 __all__ = [
-    "FlatL2Index", "FlatL1Index", "FlatChebyshevIndex", "FlatHammingIndex",
+    "FlatL2Index", "FlatL2TCIndex", "FlatL1Index", "FlatChebyshevIndex", "FlatHammingIndex",
     "VPTreeL2Index", "VPTreeL1Index", "VPTreeChebyshevIndex", "VPTreeBinaryIndex",
     "IVFFlatL2Index", "IVFFlatBinaryIndex", "kmeans_l2",
     "dist_l2", "dist_l1", "dist_chebyshev", "dist_hamming",

@@ -94,6 +94,8 @@ int upload_rows(DBuf &dst, const void *src, int64_t n, int64_t row_bytes, int st
 
 gn_index::~gn_index() {
     gn::ivf_free(this);
+    if (stream) cudaStreamSynchronize(stream);
+    if (ext && ext_free) ext_free(ext);
     if (stream) {
         cudaStreamSynchronize(stream);
         cudaStreamDestroy(stream);

@@ -34,7 +34,7 @@ struct HBuf {
     HBuf &operator=(const HBuf &) = delete;
 };
 
-enum IndexKind { K_FLAT = 1, K_IVFL2 = 2, K_IVFBIN = 3 };
+enum IndexKind { K_FLAT = 1, K_IVFL2 = 2, K_IVFBIN = 3, K_TCFLAT = 4 };
 
 struct IvfL2State;
 struct IvfBinState;
@@ -55,6 +55,8 @@ struct gn_index {
     // kind-specific state
     gn::IvfL2State *ivfl2 = nullptr;
     gn::IvfBinState *ivfbin = nullptr;
+    void *ext = nullptr;                  // other engines' state
+    void (*ext_free)(void *) = nullptr;
     ~gn_index();
 };
 

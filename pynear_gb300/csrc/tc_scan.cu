@@ -1,0 +1,509 @@
+// tc_scan.cu — tensor-core L2 candidate stage: BF16 GEMM on tcgen05 with a
+// fused per-query top-S epilogue, and the exact FP32 re-rank that follows it.
+//
+// One persistent CTA per SM walks a list of work units.  A unit is a tile of up
+// to 128 "A" rows (queries, BF16) against a range [r0, r1) of "B" rows
+// (database rows, BF16), both K-major with K padded to a multiple of 64.
+//   warp 0     TMA producer: 64-wide K slices of A (128 rows) and B (256 rows)
+//              into a 3-stage shared-memory ring (128-byte swizzle);
+//   warp 1     allocates 512 TMEM columns, one thread issues tcgen05.mma
+//              (M=128, N=256, K=16) into one of two 256-column accumulators;
+//   warps 2-5  epilogue: tcgen05.ld of the accumulator rows of their TMEM lane
+//              quadrant; score = |x|^2 - 2 q.x (exact FP32 |x|^2); each thread
+//              owns one query row and keeps its S best (score, row) keys sorted
+//              in shared memory; a float threshold rejects almost every score
+//              with one compare.
+// At the end of a unit each query's S keys go to its partial slot; the re-rank
+// kernel merges a query's slots, keeps the S best by BF16 score, recomputes
+// their distances exactly in FP32 and returns the k nearest.
+#include <cuda_bf16.h>
+
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "distance.cuh"
+#include "gemm_topk.cuh"
+#include "index.cuh"
+#include "kmeans.cuh"
+#include "tc_scan.cuh"
+#include "tc_sm100.cuh"
+#include "timing.cuh"
+#include "topk.cuh"
+
+namespace gn {
+
+constexpr int TC_M = 128, TC_N = 256, TC_BK = 64, TC_STAGES = 3;
+constexpr int TC_A_BYTES = TC_M * TC_BK * 2;   // 16 KB
+constexpr int TC_B_BYTES = TC_N * TC_BK * 2;   // 32 KB
+constexpr int TC_STAGE_BYTES = TC_A_BYTES + TC_B_BYTES;
+constexpr int TC_THREADS = 192;
+
+__host__ __device__ constexpr size_t tc_smem_bytes(int S) {
+    return 1024 /*alignment slack*/ + (size_t)TC_STAGES * TC_STAGE_BYTES + (size_t)TC_M * S * 8 + 4 * 32 * 4 + 256;
+}
+
+__device__ __forceinline__ float ord2f(uint32_t o) {
+    return __uint_as_float((o & 0x80000000u) ? (o & 0x7fffffffu) : ~o);
+}
+
+template <int S>
+__global__ void __launch_bounds__(TC_THREADS, 1)
+    tc_topk_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+                   const TcUnit *__restrict__ units, const int64_t *__restrict__ n_units_ptr, int K,
+                   const float *__restrict__ bnorm, const int64_t *__restrict__ arow_slot,
+                   uint64_t *__restrict__ part, int *__restrict__ err) {
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
+    uint8_t *stage_base = smem;
+    uint64_t *lists = reinterpret_cast<uint64_t *>(smem + TC_STAGES * TC_STAGE_BYTES);
+    float *snorm = reinterpret_cast<float *>(lists + TC_M * S);
+    uint64_t *bars = reinterpret_cast<uint64_t *>(snorm + 4 * 32);
+    uint64_t *full = bars, *empty = bars + TC_STAGES, *accfull = bars + 2 * TC_STAGES,
+             *accempty = bars + 2 * TC_STAGES + 2;
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 2 * TC_STAGES + 4);
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    volatile int *verr = err;
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < TC_STAGES; ++s) {
+            mbar_init(full + s, 1);
+            mbar_init(empty + s, 1);
+        }
+        for (int b = 0; b < 2; ++b) {
+            mbar_init(accfull + b, 1);
+            mbar_init(accempty + b, 4);
+        }
+        mbar_fence_init();
+    }
+    if (warp == 1) tmem_alloc(tmem_slot, 512);
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
+
+    const int64_t n_units = *n_units_ptr;
+    const int nk = K / TC_BK;
+
+    if (warp == 0) {
+        // ── TMA producer ──
+        if (lane == 0) {
+            uint32_t it = 0;
+            bool ok = true;
+            for (int64_t u = blockIdx.x; u < n_units && ok; u += gridDim.x) {
+                const TcUnit un = units[u];
+                const int ntile = (int)((un.r1 - un.r0 + TC_N - 1) / TC_N);
+                for (int t = 0; t < ntile && ok; ++t)
+                    for (int kb = 0; kb < nk && ok; ++kb, ++it) {
+                        const int s = it % TC_STAGES;
+                        const uint32_t ph = (it / TC_STAGES) & 1;
+                        if (!mbar_wait(empty + s, ph ^ 1, verr)) { ok = false; break; }
+                        uint8_t *sa = stage_base + s * TC_STAGE_BYTES;
+                        mbar_expect_tx(full + s, TC_STAGE_BYTES);
+                        tma_load_2d(sa, &tmA, kb * TC_BK, (int)un.a0, full + s);
+                        tma_load_2d(sa + TC_A_BYTES, &tmB, kb * TC_BK, (int)(un.r0 + (int64_t)t * TC_N), full + s);
+                    }
+            }
+        }
+    } else if (warp == 1) {
+        // ── MMA issuer ──
+        if (lane == 0) {
+            const uint32_t idesc = idesc_bf16_f32(TC_M, TC_N);
+            uint32_t it = 0, tile_it = 0;
+            bool ok = true;
+            for (int64_t u = blockIdx.x; u < n_units && ok; u += gridDim.x) {
+                const TcUnit un = units[u];
+                const int ntile = (int)((un.r1 - un.r0 + TC_N - 1) / TC_N);
+                for (int t = 0; t < ntile && ok; ++t, ++tile_it) {
+                    const int b = tile_it & 1;
+                    const uint32_t tph = (tile_it >> 1) & 1;
+                    if (!mbar_wait(accempty + b, tph ^ 1, verr)) { ok = false; break; }
+                    tc_fence_after();
+                    const uint32_t dt = tmem + (uint32_t)(b * TC_N);
+                    for (int kb = 0; kb < nk; ++kb, ++it) {
+                        const int s = it % TC_STAGES;
+                        const uint32_t ph = (it / TC_STAGES) & 1;
+                        if (!mbar_wait(full + s, ph, verr)) { ok = false; break; }
+                        tc_fence_after();
+                        const uint32_t sa = smem_u32(stage_base + s * TC_STAGE_BYTES);
+                        const uint64_t da = sdesc_sw128(sa), db = sdesc_sw128(sa + TC_A_BYTES);
+#pragma unroll
+                        for (int kk = 0; kk < TC_BK / 16; ++kk)
+                            umma_bf16(dt, da + 2 * kk, db + 2 * kk, idesc, (kb | kk) ? 1u : 0u);
+                        umma_commit(empty + s);
+                    }
+                    if (ok) umma_commit(accfull + b);
+                }
+            }
+        }
+    } else {
+        // ── epilogue: warps 2..5, TMEM lane quadrant = warp % 4 ──
+        const int quad = warp & 3;
+        const int row = quad * 32 + lane;
+        uint64_t *L = lists + row * S;
+        float *sn = snorm + (warp - 2) * 32;
+        uint32_t tile_it = 0;
+        bool ok = true;
+        for (int64_t u = blockIdx.x; u < n_units && ok; u += gridDim.x) {
+            const TcUnit un = units[u];
+            const int ntile = (int)((un.r1 - un.r0 + TC_N - 1) / TC_N);
+#pragma unroll 4
+            for (int i = 0; i < S; ++i) L[i] = KEY_EMPTY;
+            uint64_t thr = KEY_EMPTY;
+            float thr_f = __int_as_float(0x7f800000);  // +inf
+            for (int t = 0; t < ntile; ++t, ++tile_it) {
+                const int b = tile_it & 1;
+                const uint32_t tph = (tile_it >> 1) & 1;
+                if (!mbar_wait(accfull + b, tph, verr)) { ok = false; break; }
+                tc_fence_after();
+                const int64_t n0 = un.r0 + (int64_t)t * TC_N;
+                for (int c = 0; c < TC_N / 32; ++c) {
+                    const int64_t col0 = n0 + c * 32;
+                    __syncwarp();
+                    sn[lane] = (col0 + lane < un.r1) ? bnorm[col0 + lane] : 0.f;
+                    __syncwarp();
+                    float acc[32];
+                    tmem_ld32(tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(b * TC_N + c * 32), acc);
+                    const int nvalid = (int)min((int64_t)32, un.r1 - col0);
+#pragma unroll
+                    for (int j = 0; j < 32; ++j) {
+                        const float sc = fmaf(-2.f, acc[j], sn[j]);
+                        if (j < nvalid && sc <= thr_f) {
+                            const uint64_t key = make_key(f2ord(sc), (uint32_t)(col0 + j));
+                            if (key < thr) {
+                                int p = S - 1;
+                                while (p > 0 && L[p - 1] > key) { L[p] = L[p - 1]; --p; }
+                                L[p] = key;
+                                thr = L[S - 1];
+                                thr_f = (thr == KEY_EMPTY) ? __int_as_float(0x7f800000) : ord2f(key_dist(thr));
+                            }
+                        }
+                    }
+                }
+                tc_fence_before();
+                __syncwarp();
+                if (lane == 0) mbar_arrive(accempty + b);
+            }
+            if (ok && row < un.na) {
+                uint64_t *dst = part + (arow_slot[un.a0 + row] + un.rch) * S;
+#pragma unroll 4
+                for (int i = 0; i < S; ++i) dst[i] = L[i];
+            }
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (warp == 1) tmem_dealloc(tmem, 512);
+}
+
+// ── host: tensor maps and launch ──────────────────────────────────────────
+// cuTensorMapEncodeTiled, resolved through the runtime so that the library has
+// no link-time dependency on the driver library.
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                  const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static EncodeTiledFn encode_tiled() {
+    static EncodeTiledFn fn = nullptr;
+    if (!fn) {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<EncodeTiledFn>(p);
+    }
+    return fn;
+}
+
+static int make_tmap_bf16(CUtensorMap *map, const void *base, int64_t rows, int64_t K, int box_rows) {
+    EncodeTiledFn cuTensorMapEncodeTiled = encode_tiled();
+    if (!cuTensorMapEncodeTiled) return fail(GN_ERR_CUDA, "cuTensorMapEncodeTiled is unavailable");
+    cuuint64_t dims[2] = {(cuuint64_t)K, (cuuint64_t)rows};
+    cuuint64_t strides[1] = {(cuuint64_t)K * 2};
+    cuuint32_t box[2] = {(cuuint32_t)TC_BK, (cuuint32_t)box_rows};
+    cuuint32_t estr[2] = {1, 1};
+    CUresult r = cuTensorMapEncodeTiled(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void *>(base), dims,
+                                        strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                                        CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                                        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return fail(GN_ERR_CUDA, "cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
+    return GN_OK;
+}
+
+int tc_topk_launch(const TcLaunch &a, cudaStream_t st) {
+    if (a.K % TC_BK) return fail(GN_ERR_INVALID, "tensor-core scan: K must be a multiple of 64");
+    CUtensorMap ma, mb;
+    GN_TRY(make_tmap_bf16(&ma, a.A, std::max<int64_t>(a.a_rows, 1), a.K, TC_M));
+    GN_TRY(make_tmap_bf16(&mb, a.B, std::max<int64_t>(a.b_rows, 1), a.K, TC_N));
+    auto launch = [&](auto SC) {
+        constexpr int Sv = decltype(SC)::value;
+        const size_t smem = tc_smem_bytes(Sv);
+        cudaFuncSetAttribute(tc_topk_kernel<Sv>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        tc_topk_kernel<Sv><<<a.grid, TC_THREADS, smem, st>>>(ma, mb, a.units, a.n_units, a.K, a.bnorm, a.arow_slot,
+                                                              a.part, a.err);
+        return GN_OK;
+    };
+    switch (a.S) {
+    case 16: return launch(std::integral_constant<int, 16>());
+    case 32: return launch(std::integral_constant<int, 32>());
+    case 40: return launch(std::integral_constant<int, 40>());
+    case 64: return launch(std::integral_constant<int, 64>());
+    default: return fail(GN_ERR_UNSUPPORTED, "shortlist size must be 16, 32, 40 or 64");
+    }
+}
+
+// ── conversion and norms ──────────────────────────────────────────────────
+__global__ void f32_to_bf16_rows_kernel(const float *__restrict__ X, int64_t n, int d, int ldx,
+                                        __nv_bfloat16 *__restrict__ out, int K) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n * K) return;
+    const int64_t i = t / K;
+    const int j = (int)(t % K);
+    out[t] = __float2bfloat16_rn(j < d ? X[i * ldx + j] : 0.f);
+}
+
+void to_bf16_rows(const float *X, int64_t n, int d, int ldx, void *out, int K, cudaStream_t st) {
+    if (n > 0)
+        f32_to_bf16_rows_kernel<<<(unsigned)ceil_div(n * K, 256), 256, 0, st>>>(
+            X, n, d, ldx, reinterpret_cast<__nv_bfloat16 *>(out), K);
+}
+
+// ── exact re-rank ─────────────────────────────────────────────────────────
+// One warp per query: merge its nslot partial lists (S keys each, by BF16
+// score), keep the S best, recompute their L2 distance in the reference's FP32
+// order (bit-identical to the exact flat scan), return the k nearest.
+template <int RS>
+__global__ void tc_rerank_kernel(const uint64_t *__restrict__ part, int nslot, int S, const float *__restrict__ Q,
+                                 const float *__restrict__ X, int d, int dp, const int32_t *__restrict__ ids,
+                                 int64_t nq, int k, int sqrt_out, int64_t *__restrict__ out_idx,
+                                 float *__restrict__ out_dist) {
+    const int lane = threadIdx.x & 31;
+    const int64_t q = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (q >= nq) return;
+    WarpTopK<RS> L;
+    L.init();
+    uint64_t thr = KEY_EMPTY;
+    const uint64_t *p = part + q * (int64_t)nslot * S;
+    for (int sl = 0; sl < nslot; ++sl)
+        for (int j0 = 0; j0 < S; j0 += 32) {
+            const int j = j0 + lane;
+            const uint64_t key = (j < S) ? p[(int64_t)sl * S + j] : KEY_EMPTY;
+            if (__all_sync(0xffffffffu, key >= thr)) break;
+            L.offer(key, thr, S);
+        }
+    // exact distances of the shortlist, then top-k by (distance, id)
+    WarpTopK<1> F;
+    F.init();
+    uint64_t fthr = KEY_EMPTY;
+#pragma unroll
+    for (int r = 0; r < RS; ++r) {
+        const int pos = r * 32 + lane;
+        const uint64_t key = L.v[r];
+        uint64_t fk = KEY_EMPTY;
+        if (pos < S && key != KEY_EMPTY) {
+            const int64_t row = key_idx(key);
+            float dd = fdist<M_L2>(Q + q * dp, X + row * dp, d);
+            if (!sqrt_out) dd = __fmul_rn(dd, dd);
+            const uint32_t oid = ids ? (uint32_t)ids[row] : (uint32_t)row;
+            fk = make_key(__float_as_uint(dd), oid);
+        }
+        F.offer(fk, fthr, k);
+    }
+    if (lane < k) {
+        const uint64_t key = F.v[0];
+        const bool e = key == KEY_EMPTY;
+        out_idx[q * k + lane] = e ? -1 : (int64_t)key_idx(key);
+        out_dist[q * k + lane] = e ? 0.f : __uint_as_float(key_dist(key));
+    }
+}
+
+int tc_rerank_launch(const uint64_t *part, int nslot, int S, const float *Q, const float *X, int d, int dp,
+                     const int32_t *ids, int64_t nq, int k, int sqrt_out, int64_t *out_idx, float *out_dist,
+                     cudaStream_t st) {
+    if (k > 32) return fail(GN_ERR_UNSUPPORTED, "tensor-core path supports k <= 32");
+    const unsigned blocks = (unsigned)ceil_div(nq, 4);
+    if (S <= 32) tc_rerank_kernel<1><<<blocks, 128, 0, st>>>(part, nslot, S, Q, X, d, dp, ids, nq, k, sqrt_out, out_idx, out_dist);
+    else tc_rerank_kernel<2><<<blocks, 128, 0, st>>>(part, nslot, S, Q, X, d, dp, ids, nq, k, sqrt_out, out_idx, out_dist);
+    return GN_OK;
+}
+
+// ── flat tensor-core index (exact L2 via shortlist + re-rank) ─────────────
+struct TcFlatState {
+    int d = 0, dp = 0, K = 0;
+    int S = 40;
+    int64_t n = 0;
+    DBuf x32, x16, xnorm;  // fp32 rows (dp), bf16 rows (K), |x|^2
+    DBuf q32, q16, units, nunits, aslot, part, err, out_idx, out_dist;
+    int64_t planned_nq = -1;
+    int nchunks = 1, grid = 0;
+};
+
+static int tcflat_plan(TcFlatState &S, int64_t nq, cudaStream_t st) {
+    const int sms = dev_info().num_sms;
+    const int64_t qt = ceil_div(nq, TC_M);
+    // pick the number of database chunks whose unit count packs the grid best
+    int best = 1;
+    double best_eff = -1;
+    for (int c = 1; c <= 64; ++c) {
+        const int64_t rows = ceil_div(S.n, c);
+        if (c > 1 && rows < 4 * TC_N) break;
+        const int64_t units = qt * c;
+        const double eff = (double)units / (double)(ceil_div(units, sms) * sms);
+        if (eff > best_eff + 1e-3) { best_eff = eff; best = c; }
+    }
+    S.nchunks = best;
+    const int64_t rows = round_up(ceil_div(S.n, best), TC_N);
+    std::vector<TcUnit> units;
+    for (int64_t c = 0; c < best; ++c)
+        for (int64_t t = 0; t < qt; ++t) {
+            TcUnit u{};
+            u.a0 = t * TC_M;
+            u.na = (int32_t)std::min<int64_t>(TC_M, nq - u.a0);
+            u.r0 = c * rows;
+            u.r1 = std::min<int64_t>(S.n, u.r0 + rows);
+            u.rch = c;
+            if (u.r0 < u.r1) units.push_back(u);
+        }
+    std::vector<int64_t> aslot((size_t)nq);
+    for (int64_t q = 0; q < nq; ++q) aslot[(size_t)q] = q * best;
+    const int64_t nu = (int64_t)units.size();
+    GN_TRY(S.units.ensure(units.size() * sizeof(TcUnit)));
+    GN_TRY(S.nunits.ensure(8));
+    GN_TRY(S.aslot.ensure((size_t)nq * 8));
+    GN_CUDA_TRY(cudaMemcpyAsync(S.units.p, units.data(), units.size() * sizeof(TcUnit), cudaMemcpyHostToDevice, st));
+    GN_CUDA_TRY(cudaMemcpyAsync(S.nunits.p, &nu, 8, cudaMemcpyHostToDevice, st));
+    GN_CUDA_TRY(cudaMemcpyAsync(S.aslot.p, aslot.data(), (size_t)nq * 8, cudaMemcpyHostToDevice, st));
+    GN_CUDA_TRY(cudaStreamSynchronize(st));
+    S.grid = (int)std::min<int64_t>(sms, nu);
+    S.planned_nq = nq;
+    return GN_OK;
+}
+
+}  // namespace gn
+
+using namespace gn;
+
+static TcFlatState *tcs(gn_index *ix) { return reinterpret_cast<TcFlatState *>(ix->ext); }
+
+extern "C" {
+
+int gn_tcflat_create(int32_t shortlist, gn_index **out) {
+    if (!out) return fail(GN_ERR_INVALID, "out is NULL");
+    if (shortlist != 16 && shortlist != 32 && shortlist != 40 && shortlist != 64)
+        return fail(GN_ERR_INVALID, "shortlist must be 16, 32, 40 or 64");
+    gn_index *ix = new gn_index();
+    ix->kind = K_TCFLAT;
+    ix->metric = GN_METRIC_L2;
+    TcFlatState *S = new TcFlatState();
+    S->S = shortlist;
+    ix->ext = S;
+    ix->ext_free = [](void *p) { delete reinterpret_cast<TcFlatState *>(p); };
+    *out = ix;
+    return GN_OK;
+}
+
+int gn_tcflat_set(gn_index *ix, const float *data, int64_t n, int64_t d) {
+    if (!ix || ix->kind != K_TCFLAT) return fail(GN_ERR_INVALID, "not a tensor-core flat index");
+    if (n <= 0 || d <= 0 || !data) return fail(GN_ERR_INVALID, "data must be a non-empty (N, D) array");
+    if (n >= 0x7fffffffLL) return fail(GN_ERR_UNSUPPORTED, "at most 2^31-2 rows");
+    std::lock_guard<std::mutex> lk(ix->mu);
+    GN_TRY(make_stream(ix));
+    TcFlatState &S = *tcs(ix);
+    cudaStream_t st = ix->stream;
+    S.n = n;
+    S.d = (int)d;
+    S.dp = (int)round_up(d, 4);
+    S.K = (int)round_up(d, TC_BK);
+    GN_TRY(upload_rows(S.x32, data, n, d * 4, S.dp / 4, st));
+    // the BF16 copy holds at least one full 256-row TMA box
+    GN_TRY(S.x16.ensure((size_t)std::max<int64_t>(n, TC_N) * S.K * 2));
+    GN_CUDA_TRY(cudaMemsetAsync(S.x16.p, 0, (size_t)std::max<int64_t>(n, TC_N) * S.K * 2, st));
+    GN_TRY(S.xnorm.ensure((size_t)n * 4));
+    to_bf16_rows(S.x32.as<float>(), n, S.d, S.dp, S.x16.p, S.K, st);
+    row_norms(S.x32.as<float>(), n, S.dp, S.xnorm.as<float>(), st);  // |x|^2 in FP32
+    GN_TRY(S.err.ensure(4));
+    GN_CUDA_TRY(cudaMemsetAsync(S.err.p, 0, 4, st));
+    GN_CUDA_TRY(cudaStreamSynchronize(st));
+    GN_CUDA_TRY(cudaGetLastError());
+    S.planned_nq = -1;
+    ix->n = n;
+    ix->dim = d;
+    return GN_OK;
+}
+
+int gn_tcflat_search_knn_device(gn_index *ix, const float *d_queries, int64_t nq, int64_t k, int64_t *d_idx,
+                                float *d_dist, void *stream) {
+    if (!ix || ix->kind != K_TCFLAT) return fail(GN_ERR_INVALID, "not a tensor-core flat index");
+    TcFlatState &S = *tcs(ix);
+    if (S.n == 0) return fail(GN_ERR_EMPTY, "index is empty");
+    if (k <= 0 || k > 32 || k > S.S) return fail(GN_ERR_INVALID, "k must be in [1, min(32, shortlist)]");
+    if (nq <= 0) return GN_OK;
+    std::lock_guard<std::mutex> lk(ix->mu);
+    cudaStream_t st = (cudaStream_t)stream;
+    if (S.planned_nq != nq) GN_TRY(tcflat_plan(S, nq, st));
+    GN_TRY(S.q16.ensure((size_t)std::max<int64_t>(nq, TC_M) * S.K * 2));  // >= one 128-row TMA box
+    GN_TRY(S.part.ensure((size_t)nq * S.nchunks * S.S * 8));
+    to_bf16_rows(d_queries, nq, S.d, S.dp, S.q16.p, S.K, st);
+    TcLaunch a;
+    a.A = S.q16.p;
+    a.a_rows = std::max<int64_t>(nq, TC_M);
+    a.B = S.x16.p;
+    a.b_rows = std::max<int64_t>(S.n, TC_N);
+    a.K = S.K;
+    a.units = S.units.as<TcUnit>();
+    a.n_units = S.nunits.as<int64_t>();
+    a.bnorm = S.xnorm.as<float>();
+    a.arow_slot = S.aslot.as<int64_t>();
+    a.part = S.part.as<uint64_t>();
+    a.err = S.err.as<int>();
+    a.S = S.S;
+    a.grid = S.grid;
+    timing_begin(st, "tc_topk_kernel");
+    GN_TRY(tc_topk_launch(a, st));
+    timing_end(st);
+    GN_TRY(tc_rerank_launch(S.part.as<uint64_t>(), S.nchunks, S.S, d_queries, S.x32.as<float>(), S.d, S.dp,
+                            nullptr, nq, (int)k, 1, d_idx, d_dist, st));
+    GN_CUDA_TRY(cudaGetLastError());
+    return GN_OK;
+}
+
+int gn_tcflat_search_knn(gn_index *ix, const float *queries, int64_t nq, int64_t k, int64_t *out_idx,
+                         float *out_dist) {
+    if (!ix || ix->kind != K_TCFLAT) return fail(GN_ERR_INVALID, "not a tensor-core flat index");
+    TcFlatState &S = *tcs(ix);
+    if (S.n == 0) return fail(GN_ERR_EMPTY, "index is empty");
+    if (nq < 0 || (nq > 0 && (!queries || !out_idx || !out_dist))) return fail(GN_ERR_INVALID, "bad arguments");
+    if (nq == 0) return GN_OK;
+    cudaStream_t st = ix->stream;
+    {
+        std::lock_guard<std::mutex> lk(ix->mu);
+        GN_TRY(upload_rows(S.q32, queries, nq, S.d * 4, S.dp / 4, st));
+        GN_TRY(S.out_idx.ensure((size_t)nq * k * 8));
+        GN_TRY(S.out_dist.ensure((size_t)nq * k * 4));
+    }
+    GN_TRY(gn_tcflat_search_knn_device(ix, S.q32.as<float>(), nq, k, S.out_idx.as<int64_t>(), S.out_dist.as<float>(),
+                                       st));
+    GN_CUDA_TRY(cudaMemcpyAsync(out_idx, S.out_idx.p, (size_t)nq * k * 8, cudaMemcpyDeviceToHost, st));
+    GN_CUDA_TRY(cudaMemcpyAsync(out_dist, S.out_dist.p, (size_t)nq * k * 4, cudaMemcpyDeviceToHost, st));
+    GN_CUDA_TRY(cudaStreamSynchronize(st));
+    int herr = 0;
+    GN_CUDA_TRY(cudaMemcpy(&herr, S.err.p, 4, cudaMemcpyDeviceToHost));
+    if (herr) {
+        cudaMemset(S.err.p, 0, 4);
+        return fail(GN_ERR_TIMEOUT, "tensor-core scan: a pipeline wait timed out");
+    }
+    return GN_OK;
+}
+
+int gn_tc_error(gn_index *ix, int32_t *err_out) {
+    if (!ix || ix->kind != K_TCFLAT) return fail(GN_ERR_INVALID, "not a tensor-core flat index");
+    int herr = 0;
+    GN_CUDA_TRY(cudaMemcpy(&herr, tcs(ix)->err.p, 4, cudaMemcpyDeviceToHost));
+    if (err_out) *err_out = herr;
+    return GN_OK;
+}
+
+}  // extern "C"

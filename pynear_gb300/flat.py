@@ -129,6 +129,44 @@ class FlatHammingIndex(_NearestFirst):
     _binary = True
 
 
+class FlatL2TCIndex:
+    """Exact Euclidean k-NN for large batches: BF16 tensor-core shortlist of
+    `shortlist` rows per query (tcgen05 GEMM, FP32 accumulation), re-ranked with
+    the reference's FP32 L2 distance.  Results are nearest-first and equal the
+    exact scan whenever the true k nearest rows are in the shortlist; k <= 32.
+    """
+
+    def __init__(self, shortlist: int = 40) -> None:
+        self._h = _lib.Handle("gn_tcflat_create", int(shortlist))
+        self._n = 0
+        self._dim = 0
+
+    def set(self, vectors) -> None:
+        arr = _as_float2d(vectors, "set")
+        _lib.call("gn_tcflat_set", self._h.h, _lib.ptr(arr), arr.shape[0], arr.shape[1])
+        self._n, self._dim = arr.shape
+
+    def search_knn_arrays(self, queries, k: int):
+        q = _as_float2d(queries, "searchKNN")
+        if self._n and q.shape[1] != self._dim:
+            raise ValueError("invalid data dimension: index and query dimensions must agree")
+        k = int(k)
+        nq = q.shape[0]
+        idx = np.empty((nq, k), np.int64)
+        dist = np.empty((nq, k), np.float32)
+        if nq or self._n == 0:
+            _lib.call("gn_tcflat_search_knn", self._h.h, _lib.ptr(q), nq, k, _lib.ptr(idx), _lib.ptr(dist))
+        return idx, dist
+
+    def searchKNN(self, queries, k: int):
+        idx, dist = self.search_knn_arrays(queries, k)
+        return idx.tolist(), dist.tolist()
+
+    def search1NN(self, queries):
+        idx, dist = self.search_knn_arrays(queries, 1)
+        return idx[:, 0].tolist(), dist[:, 0].tolist()
+
+
 class _VPTreeCompat(_FlatBase):
     """Reference-compatible surface: searchKNN returns farthest-first."""
 

@@ -1,0 +1,41 @@
+"""Tensor-core shortlist (BF16 tcgen05 GEMM + top-S) followed by the exact FP32
+re-rank: results must equal the exact flat scan (indices and the reference's
+distance bits) and match an FP64 oracle within FP32 rounding."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def mixture(n, d, nc, nq, seed):
+    rng = np.random.default_rng(seed)
+    c = rng.standard_normal((nc, d), dtype=np.float32)
+    db = (c[rng.integers(0, nc, n)] + np.float32(0.3) * rng.standard_normal((n, d), dtype=np.float32))
+    q = (c[rng.integers(0, nc, nq)] + np.float32(0.3) * rng.standard_normal((nq, d), dtype=np.float32))
+    return db.astype(np.float32), q.astype(np.float32)
+
+
+@pytest.mark.parametrize("n,d,nq,k,S", [(4096, 128, 128, 10, 40), (50_000, 128, 300, 10, 40),
+                                        (30_001, 64, 77, 5, 32), (20_000, 200, 129, 1, 16)])
+def test_tc_shortlist_equals_exact(gn, oracle, n, d, nq, k, S):
+    db, q = mixture(n, d, 256, nq, seed=n + d)
+    tc = gn.FlatL2TCIndex(shortlist=S)
+    tc.set(db)
+    idx, dist = tc.search_knn_arrays(q, k)
+    ex = gn.FlatL2Index()
+    ex.set(db)
+    ei, ed = ex.search_knn_arrays(q, k)
+    assert np.array_equal(idx, ei)
+    assert np.array_equal(dist.view(np.uint32), ed.view(np.uint32))
+    oi, od = oracle.knn_l2sq_f64(db, q[:64], k)
+    err = np.abs(dist[:64].astype(np.float64) - np.sqrt(od))
+    assert err.max() <= 1e-5 * np.sqrt(od).max()
+
+
+def test_tc_small_batches_and_tiny_db(gn, oracle):
+    db, q = mixture(300, 128, 8, 3, seed=5)
+    tc = gn.FlatL2TCIndex(shortlist=40)
+    tc.set(db)
+    idx, dist = tc.search_knn_arrays(q, 10)
+    oi, od = oracle.knn_float("l2", db, q, 10)
+    assert np.array_equal(idx, oi)
