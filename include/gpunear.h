@@ -123,6 +123,15 @@ int gn_ivfl2_search_knn(gn_index *ix, const float *queries, int64_t nq, int64_t 
 int gn_ivfl2_search_knn_device(gn_index *ix, const float *d_queries, int64_t nq, int64_t k, int64_t *d_idx,
                                float *d_dist, int64_t *d_cnt, void *stream);
 int gn_ivfl2_set_n_probe(gn_index *ix, int32_t n_probe);
+/* Search engine (no reference counterpart; same result contract):
+ *   mode 0  FP32 CUDA-core scan, distances |q|^2 + |x|^2 - 2 q.x clamped at 0,
+ *           the formula of forest.py:189-194;
+ *   mode 1  BF16 tcgen05 GEMM keeps `shortlist` candidates per query over the
+ *           probed lists, re-ranked with the exact squared L2 in FP32
+ *           (compensated sum); k <= min(32, shortlist). */
+int gn_ivfl2_set_mode(gn_index *ix, int32_t mode, int32_t shortlist);
+/* error word of the last tensor-core launch (nonzero: a bounded wait expired) */
+int gn_ivfl2_error(gn_index *ix, int32_t *err_out);
 int gn_ivfl2_info(gn_index *ix, int32_t *n_clusters_built, int32_t *n_probe, int64_t *n, int64_t *d);
 /* copy out the built state: centroids (n_clusters_built*d), list offsets
  * (n_clusters_built+1, int64), original ids in list order (n, int64) */

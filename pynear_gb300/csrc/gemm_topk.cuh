@@ -26,6 +26,10 @@ __device__ __forceinline__ uint32_t f2ord(float f) {
     return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
 }
 
+__device__ __forceinline__ float ord2f(uint32_t o) {
+    return __uint_as_float((o & 0x80000000u) ? (o & 0x7fffffffu) : ~o);
+}
+
 // Load one BK-wide slice of the A tile (rows arow[0..BM), gathered) and the B
 // tile (rows b0..b0+BN) into shared buffer `buf`.  Rows past the end read 0.
 __device__ __forceinline__ void gt_load(GemmTileSmem &s, int buf, const float *__restrict__ A,

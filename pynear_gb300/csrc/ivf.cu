@@ -460,12 +460,12 @@ static int64_t max_slots_per_query(const std::vector<int64_t> &top, int np, int 
     return p + (top[(size_t)p] + rc - 1) / rc;
 }
 
-// Common bucket/plan/scan/merge sequence.  probes (int32, nq*np) must be
-// filled.  scan_launch(grid) launches the metric's scan kernel.
-template <typename ScanLaunch>
-static int ivf_run_lists(IvfScratch &S, int64_t nq, int np, int nc, const int64_t *d_list_off, int rc, int qchunk,
-                         int k, int is_hamming, int64_t *d_idx, void *d_dist, int64_t *d_cnt, int grid,
-                         ScanLaunch &&scan_launch, cudaStream_t st) {
+// Bucket the (query, probe) pairs by list and plan the work items; probes
+// (int32, nq*np) must be filled.  Produces boff, bucket, item_off, slot_rel,
+// qslot in S.  All on the device, no host synchronisation.
+int ivf_plan(IvfScratch &S, int64_t nq, int np, int nc, const int64_t *d_list_off, int rc, int qchunk,
+             cudaStream_t st, int slot_rc) {
+    if (slot_rc <= 0) slot_rc = rc;
     const int64_t npairs = nq * np;
     GN_TRY(S.bcnt.ensure((size_t)nc * 4));
     GN_TRY(S.fill.ensure((size_t)nc * 4));
@@ -485,9 +485,20 @@ static int ivf_run_lists(IvfScratch &S, int64_t nq, int np, int nc, const int64_
                                         S.item_off.as<int64_t>());
     ivf_bucket_fill_kernel<<<pb, 256, 0, st>>>(S.probes.as<int32_t>(), npairs, S.boff.as<int64_t>(),
                                                S.fill.as<int32_t>(), S.bucket.as<int64_t>());
-    ivf_slots_kernel<<<(unsigned)ceil_div(nq, 128), 128, 0, st>>>(S.probes.as<int32_t>(), nq, np, d_list_off, rc,
-                                                                  S.slot_rel.as<int64_t>(), S.qcount.as<int64_t>());
+    ivf_slots_kernel<<<(unsigned)ceil_div(nq, 128), 128, 0, st>>>(S.probes.as<int32_t>(), nq, np, d_list_off,
+                                                                  slot_rc, S.slot_rel.as<int64_t>(),
+                                                                  S.qcount.as<int64_t>());
     ivf_qscan_kernel<<<1, 1024, 0, st>>>(S.qcount.as<int64_t>(), nq, S.qslot.as<int64_t>());
+    GN_CUDA_TRY(cudaGetLastError());
+    return GN_OK;
+}
+
+// Plan, run the metric's scan kernel (scan_launch(grid)), merge the slots.
+template <typename ScanLaunch>
+static int ivf_run_lists(IvfScratch &S, int64_t nq, int np, int nc, const int64_t *d_list_off, int rc, int qchunk,
+                         int k, int is_hamming, int64_t *d_idx, void *d_dist, int64_t *d_cnt, int grid,
+                         ScanLaunch &&scan_launch, cudaStream_t st) {
+    GN_TRY(ivf_plan(S, nq, np, nc, d_list_off, rc, qchunk, st));
     timing_begin(st, is_hamming ? "ivfbin_scan_kernel" : "ivf_scan_kernel");
     GN_TRY(scan_launch(grid));
     timing_end(st);
@@ -497,6 +508,10 @@ static int ivf_run_lists(IvfScratch &S, int64_t nq, int np, int nc, const int64_
                                                                        nq, k, is_hamming, d_idx, d_dist, d_cnt);
         return GN_OK;
     });
+}
+
+int64_t ivf_max_slots_per_query(const std::vector<int64_t> &top, int np, int rc) {
+    return max_slots_per_query(top, np, rc);
 }
 
 // ── float IVF: build ──────────────────────────────────────────────────────
@@ -517,6 +532,7 @@ static int ivfl2_build_from_labels(gn_index *ix, const float *dX, int64_t n, int
     std::vector<int32_t> perm;
     csr_from_labels(labels, ncent, order, perm, S.h_off);
     S.nc = (int32_t)order.size();
+    S.K = 0;  // BF16 copy for the tensor-core engine is rebuilt on first use
     S.n = n;
     S.d = d;
     S.dp = dp;
@@ -543,6 +559,21 @@ static int ivfl2_build_from_labels(gn_index *ix, const float *dX, int64_t n, int
     return GN_OK;
 }
 
+// Coarse probing of a float IVF: qn = |q|^2, probes = the np nearest lists.
+int ivfl2_coarse(gn_index *ix, const float *dQ, int64_t nq, int np, cudaStream_t st) {
+    IvfL2State &S = *ix->ivfl2;
+    IvfScratch &T = S.s;
+    GN_TRY(T.qn.ensure((size_t)nq * 4));
+    GN_TRY(T.probes.ensure((size_t)nq * np * 4));
+    row_norms(dQ, nq, S.dp, T.qn.as<float>(), st);
+    return dispatch_r(np, [&](auto RC) {
+        constexpr int R = decltype(RC)::value;
+        ivf_coarse_kernel<R><<<(unsigned)ceil_div(nq, GT_BM), GT_THREADS, 0, st>>>(
+            dQ, T.qn.as<float>(), nq, S.dp, S.cent.as<float>(), S.cnorm.as<float>(), S.nc, np, T.probes.as<int32_t>());
+        return GN_OK;
+    });
+}
+
 // ── float IVF: search on device buffers ───────────────────────────────────
 static int ivfl2_search_dev(gn_index *ix, const float *dQ, int64_t nq, int k, int64_t *d_idx, float *d_dist,
                             int64_t *d_cnt, cudaStream_t st) {
@@ -552,15 +583,8 @@ static int ivfl2_search_dev(gn_index *ix, const float *dQ, int64_t nq, int k, in
     if (np <= 0) return fail(GN_ERR_INVALID, "n_probe must be positive");
     if (np > 256) return fail(GN_ERR_UNSUPPORTED, "n_probe > 256 is not supported");
     if (nq == 0) return GN_OK;
-    GN_TRY(T.qn.ensure((size_t)nq * 4));
-    GN_TRY(T.probes.ensure((size_t)nq * np * 4));
-    row_norms(dQ, nq, S.dp, T.qn.as<float>(), st);
-    GN_TRY(dispatch_r(np, [&](auto RC) {
-        constexpr int R = decltype(RC)::value;
-        ivf_coarse_kernel<R><<<(unsigned)ceil_div(nq, GT_BM), GT_THREADS, 0, st>>>(
-            dQ, T.qn.as<float>(), nq, S.dp, S.cent.as<float>(), S.cnorm.as<float>(), S.nc, np, T.probes.as<int32_t>());
-        return GN_OK;
-    }));
+    if (S.mode == 1) return ivfl2_search_tc(ix, dQ, nq, k, d_idx, d_dist, d_cnt, st);
+    GN_TRY(ivfl2_coarse(ix, dQ, nq, np, st));
     const int64_t slots = nq * max_slots_per_query(S.top_rows, np, S.rc);
     GN_TRY(T.part.ensure((size_t)slots * k * 8));
     if (!g_scan_blocks_l2) {

@@ -26,6 +26,13 @@ struct IvfL2State {
     std::vector<int64_t> top_rows;  // top_rows[p] = rows in the p largest lists
     int rc = 1024;               // rows per scan work item
     IvfScratch s;
+    // tensor-core engine (mode 1): BF16 rows in list order, shortlist + re-rank
+    int mode = 0;                // 0 FP32 CUDA-core scan, 1 BF16 tcgen05 shortlist + exact FP32 re-rank
+    int shortlist = 40;
+    int K = 0;                   // BF16 row length, round_up(d, 64)
+    int rc_tc = 4096;            // list rows per tensor-core work unit
+    DBuf x16;                    // n*K BF16 rows, list order
+    DBuf qb, aslot, units, nunits, err, scores;
 };
 
 // Binary IVF (IVFFlatBinaryIndex semantics).
@@ -44,5 +51,15 @@ struct IvfBinState {
     int rc = 4096;
     IvfScratch s;
 };
+
+// slot_rc: rows per partial slot (defaults to rc); 1 makes every (query, probe)
+// own a segment of one entry per list row (the tensor-core store mode).
+int ivf_plan(IvfScratch &S, int64_t nq, int np, int nc, const int64_t *d_list_off, int rc, int qchunk,
+             cudaStream_t st, int slot_rc = 0);
+int64_t ivf_max_slots_per_query(const std::vector<int64_t> &top, int np, int rc);
+int ivfl2_coarse(gn_index *ix, const float *dQ, int64_t nq, int np, cudaStream_t st);
+int ivfl2_search_tc(gn_index *ix, const float *dQ, int64_t nq, int k, int64_t *d_idx, float *d_dist, int64_t *d_cnt,
+                    cudaStream_t st);
+int ivfl2_prepare_tc(gn_index *ix, cudaStream_t st);
 
 }  // namespace gn

@@ -37,28 +37,38 @@ constexpr int TC_M = 128, TC_N = 256, TC_BK = 64, TC_STAGES = 3;
 constexpr int TC_A_BYTES = TC_M * TC_BK * 2;   // 16 KB
 constexpr int TC_B_BYTES = TC_N * TC_BK * 2;   // 32 KB
 constexpr int TC_STAGE_BYTES = TC_A_BYTES + TC_B_BYTES;
-constexpr int TC_THREADS = 192;
+// Epilogue warps: 4 in top-S mode (one per TMEM lane quadrant, each thread
+// owns a query row's list), 8 in store mode (two per quadrant, each covering
+// half of the accumulator's columns).
+__host__ __device__ constexpr int tc_nepi(int S) { return S ? 4 : 8; }
+__host__ __device__ constexpr int tc_threads(int S) { return 64 + 32 * tc_nepi(S); }
 
 __host__ __device__ constexpr size_t tc_smem_bytes(int S) {
-    return 1024 /*alignment slack*/ + (size_t)TC_STAGES * TC_STAGE_BYTES + (size_t)TC_M * S * 8 + 4 * 32 * 4 + 256;
-}
-
-__device__ __forceinline__ float ord2f(uint32_t o) {
-    return __uint_as_float((o & 0x80000000u) ? (o & 0x7fffffffu) : ~o);
+    // S == 0 is the store mode: a 32x33 transpose tile per epilogue warp
+    return 1024 /*alignment slack*/ + (size_t)TC_STAGES * TC_STAGE_BYTES +
+           (S ? (size_t)TC_M * S * 8 + (size_t)TC_M * 32 * 5 : (size_t)tc_nepi(S) * 32 * 33 * 4) +
+           (size_t)tc_nepi(S) * 32 * 4 + 256;
 }
 
 template <int S>
-__global__ void __launch_bounds__(TC_THREADS, 1)
+__global__ void __launch_bounds__(tc_threads(S), 1)
     tc_topk_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
-                   const TcUnit *__restrict__ units, const int64_t *__restrict__ n_units_ptr, int K,
+                   const TcUnit *__restrict__ units, const int64_t *__restrict__ n_units_ptr,
+                   const int64_t *__restrict__ cta_off, int K,
                    const float *__restrict__ bnorm, const int64_t *__restrict__ arow_slot,
-                   uint64_t *__restrict__ part, int *__restrict__ err) {
+                   uint64_t *__restrict__ part, float *__restrict__ scores, int *__restrict__ err) {
+    constexpr bool STORE = (S == 0);
+    constexpr int SL = STORE ? 1 : S;  // list length used for shared-memory layout
+    constexpr int NEPI = tc_nepi(S);
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
     uint8_t *stage_base = smem;
     uint64_t *lists = reinterpret_cast<uint64_t *>(smem + TC_STAGES * TC_STAGE_BYTES);
-    float *snorm = reinterpret_cast<float *>(lists + TC_M * S);
-    uint64_t *bars = reinterpret_cast<uint64_t *>(snorm + 4 * 32);
+    float *cand_s = reinterpret_cast<float *>(lists + TC_M * SL);        // [32][TC_M]
+    uint8_t *cand_j = reinterpret_cast<uint8_t *>(cand_s + 32 * TC_M);   // [32][TC_M]
+    float *xpose = reinterpret_cast<float *>(smem + TC_STAGES * TC_STAGE_BYTES);  // store mode: [NEPI][32][33]
+    float *snorm = STORE ? xpose + NEPI * 32 * 33 : reinterpret_cast<float *>(cand_j + 32 * TC_M);
+    uint64_t *bars = reinterpret_cast<uint64_t *>(snorm + NEPI * 32);
     uint64_t *full = bars, *empty = bars + TC_STAGES, *accfull = bars + 2 * TC_STAGES,
              *accempty = bars + 2 * TC_STAGES + 2;
     uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 2 * TC_STAGES + 4);
@@ -73,7 +83,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         }
         for (int b = 0; b < 2; ++b) {
             mbar_init(accfull + b, 1);
-            mbar_init(accempty + b, 4);
+            mbar_init(accempty + b, NEPI);
         }
         mbar_fence_init();
     }
@@ -83,7 +93,14 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     tc_fence_after();
     const uint32_t tmem = *tmem_slot;
 
+    // this CTA's units: [u_begin, u_end) with stride u_step
     const int64_t n_units = *n_units_ptr;
+    int64_t u_begin = blockIdx.x, u_end = n_units, u_step = gridDim.x;
+    if (cta_off) {
+        u_begin = cta_off[blockIdx.x];
+        u_end = cta_off[blockIdx.x + 1];
+        u_step = 1;
+    }
     const int nk = K / TC_BK;
 
     if (warp == 0) {
@@ -91,7 +108,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         if (lane == 0) {
             uint32_t it = 0;
             bool ok = true;
-            for (int64_t u = blockIdx.x; u < n_units && ok; u += gridDim.x) {
+            for (int64_t u = u_begin; u < u_end && ok; u += u_step) {
                 const TcUnit un = units[u];
                 const int ntile = (int)((un.r1 - un.r0 + TC_N - 1) / TC_N);
                 for (int t = 0; t < ntile && ok; ++t)
@@ -112,7 +129,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             const uint32_t idesc = idesc_bf16_f32(TC_M, TC_N);
             uint32_t it = 0, tile_it = 0;
             bool ok = true;
-            for (int64_t u = blockIdx.x; u < n_units && ok; u += gridDim.x) {
+            for (int64_t u = u_begin; u < u_end && ok; u += u_step) {
                 const TcUnit un = units[u];
                 const int ntile = (int)((un.r1 - un.r0 + TC_N - 1) / TC_N);
                 for (int t = 0; t < ntile && ok; ++t, ++tile_it) {
@@ -137,47 +154,120 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 }
             }
         }
-    } else {
-        // ── epilogue: warps 2..5, TMEM lane quadrant = warp % 4 ──
+    } else if constexpr (STORE) {
+        // ── epilogue (store mode): scores of a 32x32 block go through a padded
+        // shared tile so that each store instruction writes 32 consecutive
+        // floats of one query's segment ──
         const int quad = warp & 3;
-        const int row = quad * 32 + lane;
-        uint64_t *L = lists + row * S;
+        const int grp = (warp - 2) >> 2;  // which half of the 256 columns
+        constexpr int CPG = (TC_N / 32) / (NEPI / 4);
+        float *xp = xpose + (warp - 2) * 32 * 33;
         float *sn = snorm + (warp - 2) * 32;
         uint32_t tile_it = 0;
         bool ok = true;
-        for (int64_t u = blockIdx.x; u < n_units && ok; u += gridDim.x) {
+        for (int64_t u = u_begin; u < u_end && ok; u += u_step) {
+            const TcUnit un = units[u];
+            const int ntile = (int)((un.r1 - un.r0 + TC_N - 1) / TC_N);
+            // segment base of each of this warp's 32 query rows (lane r holds row r's)
+            const int qrow = quad * 32 + lane;
+            const int64_t myseg = (qrow < un.na) ? arow_slot[un.a0 + qrow] - un.rbase : INT64_MIN;
+            for (int t = 0; t < ntile; ++t, ++tile_it) {
+                const int b = tile_it & 1;
+                const uint32_t tph = (tile_it >> 1) & 1;
+                const int64_t n0 = un.r0 + (int64_t)t * TC_N;
+                float nrm[CPG];
+#pragma unroll
+                for (int cc = 0; cc < CPG; ++cc) {
+                    const int64_t col = n0 + (grp * CPG + cc) * 32 + lane;
+                    nrm[cc] = col < un.r1 ? __ldg(bnorm + col) : 0.f;
+                }
+                if (!mbar_wait(accfull + b, tph, verr)) { ok = false; break; }
+                tc_fence_after();
+#pragma unroll 1
+                for (int cc = 0; cc < CPG; ++cc) {
+                    const int c = grp * CPG + cc;
+                    const int64_t col0 = n0 + c * 32;
+                    __syncwarp();
+                    sn[lane] = nrm[cc];
+                    __syncwarp();
+                    float acc[32];
+                    tmem_ld32(tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(b * TC_N + c * 32), acc);
+#pragma unroll
+                    for (int j = 0; j < 32; ++j) xp[lane * 33 + j] = fmaf(-2.f, acc[j], sn[j]);
+                    __syncwarp();
+                    const bool colok = col0 + lane < un.r1;
+#pragma unroll 4
+                    for (int r = 0; r < 32; ++r) {
+                        const int64_t seg = __shfl_sync(0xffffffffu, myseg, r);
+                        if (seg != INT64_MIN && colok) scores[seg + col0 + lane] = xp[r * 33 + lane];
+                    }
+                }
+                tc_fence_before();
+                __syncwarp();
+                if (lane == 0) mbar_arrive(accempty + b);
+            }
+        }
+    } else {
+        // ── epilogue: warps 2..5, TMEM lane quadrant = warp % 4 ──
+        // list entry i of query row r lives at lists[i * TC_M + r] (bank-conflict free)
+        const int quad = warp & 3;
+        const int row = quad * 32 + lane;
+        uint64_t *L = lists + row;
+        float *sn = snorm + (warp - 2) * 32;
+        uint32_t tile_it = 0;
+        bool ok = true;
+        for (int64_t u = u_begin; u < u_end && ok; u += u_step) {
             const TcUnit un = units[u];
             const int ntile = (int)((un.r1 - un.r0 + TC_N - 1) / TC_N);
 #pragma unroll 4
-            for (int i = 0; i < S; ++i) L[i] = KEY_EMPTY;
+            for (int i = 0; i < S; ++i) L[i * TC_M] = KEY_EMPTY;
             uint64_t thr = KEY_EMPTY;
             float thr_f = __int_as_float(0x7f800000);  // +inf
             for (int t = 0; t < ntile; ++t, ++tile_it) {
                 const int b = tile_it & 1;
                 const uint32_t tph = (tile_it >> 1) & 1;
+                const int64_t n0 = un.r0 + (int64_t)t * TC_N;
+                // row norms of this tile's 256 columns, fetched before the wait
+                float nrm[TC_N / 32];
+#pragma unroll
+                for (int c = 0; c < TC_N / 32; ++c) {
+                    const int64_t col = n0 + c * 32 + lane;
+                    nrm[c] = col < un.r1 ? __ldg(bnorm + col) : 0.f;
+                }
                 if (!mbar_wait(accfull + b, tph, verr)) { ok = false; break; }
                 tc_fence_after();
-                const int64_t n0 = un.r0 + (int64_t)t * TC_N;
+#pragma unroll 1
                 for (int c = 0; c < TC_N / 32; ++c) {
                     const int64_t col0 = n0 + c * 32;
                     __syncwarp();
-                    sn[lane] = (col0 + lane < un.r1) ? bnorm[col0 + lane] : 0.f;
+                    sn[lane] = nrm[c];
                     __syncwarp();
                     float acc[32];
                     tmem_ld32(tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(b * TC_N + c * 32), acc);
                     const int nvalid = (int)min((int64_t)32, un.r1 - col0);
+                    // branch-free filter: passing scores go to this thread's
+                    // candidate column in shared memory
+                    int cnt = 0;
 #pragma unroll
                     for (int j = 0; j < 32; ++j) {
                         const float sc = fmaf(-2.f, acc[j], sn[j]);
-                        if (j < nvalid && sc <= thr_f) {
-                            const uint64_t key = make_key(f2ord(sc), (uint32_t)(col0 + j));
-                            if (key < thr) {
-                                int p = S - 1;
-                                while (p > 0 && L[p - 1] > key) { L[p] = L[p - 1]; --p; }
-                                L[p] = key;
-                                thr = L[S - 1];
-                                thr_f = (thr == KEY_EMPTY) ? __int_as_float(0x7f800000) : ord2f(key_dist(thr));
-                            }
+                        const bool pass = (j < nvalid) && (sc <= thr_f);
+                        if (pass) {
+                            cand_s[cnt * TC_M + row] = sc;
+                            cand_j[cnt * TC_M + row] = (uint8_t)j;
+                        }
+                        cnt += pass ? 1 : 0;
+                    }
+#pragma unroll 1
+                    for (int i = 0; i < cnt; ++i) {
+                        const uint64_t key =
+                            make_key(f2ord(cand_s[i * TC_M + row]), (uint32_t)(col0 + cand_j[i * TC_M + row]));
+                        if (key < thr) {
+                            int p = S - 1;
+                            while (p > 0 && L[(p - 1) * TC_M] > key) { L[p * TC_M] = L[(p - 1) * TC_M]; --p; }
+                            L[p * TC_M] = key;
+                            thr = L[(S - 1) * TC_M];
+                            thr_f = (thr == KEY_EMPTY) ? __int_as_float(0x7f800000) : ord2f(key_dist(thr));
                         }
                     }
                 }
@@ -188,7 +278,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             if (ok && row < un.na) {
                 uint64_t *dst = part + (arow_slot[un.a0 + row] + un.rch) * S;
 #pragma unroll 4
-                for (int i = 0; i < S; ++i) dst[i] = L[i];
+                for (int i = 0; i < S; ++i) dst[i] = L[i * TC_M];
             }
         }
     }
@@ -242,11 +332,12 @@ int tc_topk_launch(const TcLaunch &a, cudaStream_t st) {
         constexpr int Sv = decltype(SC)::value;
         const size_t smem = tc_smem_bytes(Sv);
         cudaFuncSetAttribute(tc_topk_kernel<Sv>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        tc_topk_kernel<Sv><<<a.grid, TC_THREADS, smem, st>>>(ma, mb, a.units, a.n_units, a.K, a.bnorm, a.arow_slot,
-                                                              a.part, a.err);
+        tc_topk_kernel<Sv><<<a.grid, tc_threads(Sv), smem, st>>>(ma, mb, a.units, a.n_units, a.cta_off, a.K, a.bnorm,
+                                                              a.arow_slot, a.part, a.scores, a.err);
         return GN_OK;
     };
     switch (a.S) {
+    case 0: return launch(std::integral_constant<int, 0>());
     case 16: return launch(std::integral_constant<int, 16>());
     case 32: return launch(std::integral_constant<int, 32>());
     case 40: return launch(std::integral_constant<int, 40>());
@@ -336,48 +427,56 @@ struct TcFlatState {
     int S = 40;
     int64_t n = 0;
     DBuf x32, x16, xnorm;  // fp32 rows (dp), bf16 rows (K), |x|^2
-    DBuf q32, q16, units, nunits, aslot, part, err, out_idx, out_dist;
+    DBuf q32, q16, units, nunits, ctaoff, aslot, part, err, out_idx, out_dist;
     int64_t planned_nq = -1;
     int nchunks = 1, grid = 0;
 };
 
+// Split the (query tile, database tile) space into one contiguous run per CTA,
+// cut at query-tile boundaries: each CTA keeps its per-query lists over
+// thousands of tiles, so list insertions stay rare.
 static int tcflat_plan(TcFlatState &S, int64_t nq, cudaStream_t st) {
     const int sms = dev_info().num_sms;
     const int64_t qt = ceil_div(nq, TC_M);
-    // pick the number of database chunks whose unit count packs the grid best
-    int best = 1;
-    double best_eff = -1;
-    for (int c = 1; c <= 64; ++c) {
-        const int64_t rows = ceil_div(S.n, c);
-        if (c > 1 && rows < 4 * TC_N) break;
-        const int64_t units = qt * c;
-        const double eff = (double)units / (double)(ceil_div(units, sms) * sms);
-        if (eff > best_eff + 1e-3) { best_eff = eff; best = c; }
-    }
-    S.nchunks = best;
-    const int64_t rows = round_up(ceil_div(S.n, best), TC_N);
+    const int64_t nt = ceil_div(S.n, TC_N);
+    const int64_t total = qt * nt;
+    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(sms, total));
     std::vector<TcUnit> units;
-    for (int64_t c = 0; c < best; ++c)
-        for (int64_t t = 0; t < qt; ++t) {
+    std::vector<int64_t> cta_off((size_t)grid + 1, 0);
+    std::vector<int32_t> seg((size_t)qt, 0);
+    for (int g = 0; g < grid; ++g) {
+        const int64_t b = total * g / grid, e = total * (g + 1) / grid;
+        int64_t p = b;
+        while (p < e) {
+            const int64_t t = p / nt;
+            const int64_t te = std::min(e, (t + 1) * nt);
             TcUnit u{};
             u.a0 = t * TC_M;
             u.na = (int32_t)std::min<int64_t>(TC_M, nq - u.a0);
-            u.r0 = c * rows;
-            u.r1 = std::min<int64_t>(S.n, u.r0 + rows);
-            u.rch = c;
-            if (u.r0 < u.r1) units.push_back(u);
+            u.r0 = (p - t * nt) * TC_N;
+            u.r1 = std::min<int64_t>(S.n, (te - t * nt) * TC_N);
+            u.rch = seg[(size_t)t]++;
+            units.push_back(u);
+            p = te;
         }
+        cta_off[(size_t)g + 1] = (int64_t)units.size();
+    }
+    int32_t nslot = 1;
+    for (int32_t v : seg) nslot = std::max(nslot, v);
+    S.nchunks = nslot;
     std::vector<int64_t> aslot((size_t)nq);
-    for (int64_t q = 0; q < nq; ++q) aslot[(size_t)q] = q * best;
+    for (int64_t q = 0; q < nq; ++q) aslot[(size_t)q] = q * nslot;
     const int64_t nu = (int64_t)units.size();
     GN_TRY(S.units.ensure(units.size() * sizeof(TcUnit)));
     GN_TRY(S.nunits.ensure(8));
+    GN_TRY(S.ctaoff.ensure(cta_off.size() * 8));
     GN_TRY(S.aslot.ensure((size_t)nq * 8));
     GN_CUDA_TRY(cudaMemcpyAsync(S.units.p, units.data(), units.size() * sizeof(TcUnit), cudaMemcpyHostToDevice, st));
     GN_CUDA_TRY(cudaMemcpyAsync(S.nunits.p, &nu, 8, cudaMemcpyHostToDevice, st));
+    GN_CUDA_TRY(cudaMemcpyAsync(S.ctaoff.p, cta_off.data(), cta_off.size() * 8, cudaMemcpyHostToDevice, st));
     GN_CUDA_TRY(cudaMemcpyAsync(S.aslot.p, aslot.data(), (size_t)nq * 8, cudaMemcpyHostToDevice, st));
     GN_CUDA_TRY(cudaStreamSynchronize(st));
-    S.grid = (int)std::min<int64_t>(sms, nu);
+    S.grid = grid;
     S.planned_nq = nq;
     return GN_OK;
 }
@@ -447,6 +546,8 @@ int gn_tcflat_search_knn_device(gn_index *ix, const float *d_queries, int64_t nq
     GN_TRY(S.q16.ensure((size_t)std::max<int64_t>(nq, TC_M) * S.K * 2));  // >= one 128-row TMA box
     GN_TRY(S.part.ensure((size_t)nq * S.nchunks * S.S * 8));
     to_bf16_rows(d_queries, nq, S.d, S.dp, S.q16.p, S.K, st);
+    // slots of a query tile covered by fewer runs than the maximum stay empty
+    GN_CUDA_TRY(cudaMemsetAsync(S.part.p, 0xff, (size_t)nq * S.nchunks * S.S * 8, st));
     TcLaunch a;
     a.A = S.q16.p;
     a.a_rows = std::max<int64_t>(nq, TC_M);
@@ -455,6 +556,7 @@ int gn_tcflat_search_knn_device(gn_index *ix, const float *d_queries, int64_t nq
     a.K = S.K;
     a.units = S.units.as<TcUnit>();
     a.n_units = S.nunits.as<int64_t>();
+    a.cta_off = S.ctaoff.as<int64_t>();
     a.bnorm = S.xnorm.as<float>();
     a.arow_slot = S.aslot.as<int64_t>();
     a.part = S.part.as<uint64_t>();

@@ -11,6 +11,7 @@ struct TcUnit {
     int64_t a0;
     int64_t r0;
     int64_t r1;
+    int64_t rbase;  // store mode: first B row of the list the unit belongs to
     int32_t na;
     int32_t rch;
 };
@@ -23,12 +24,16 @@ struct TcLaunch {
     int K = 0;                // multiple of 64
     const TcUnit *units = nullptr;
     const int64_t *n_units = nullptr;  // device scalar
+    const int64_t *cta_off = nullptr;  // optional [grid+1] unit range per CTA (else strided)
     const float *bnorm = nullptr;      // |B row|^2, FP32
     const int64_t *arow_slot = nullptr;
     uint64_t *part = nullptr;          // slots x S keys
     int *err = nullptr;                // device error word (0 = ok)
     int S = 40;
     int grid = 0;
+    // store mode (S == 0): write every score instead of keeping the top S;
+    // query row a0 + i stores column c at scores[arow_slot[a0 + i] + c - rbase]
+    float *scores = nullptr;
 };
 
 int tc_topk_launch(const TcLaunch &a, cudaStream_t st);

@@ -43,12 +43,14 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
 __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, volatile int *err) {
     if (mbar_try_wait(bar, parity)) return true;
     const long long t0 = clock64();
-    for (;;) {
+    for (uint32_t i = 1;; ++i) {
         if (mbar_try_wait(bar, parity)) return true;
-        if (*err) return false;
-        if (clock64() - t0 > TC_TIMEOUT_CYCLES) {
-            atomicExch((int *)err, 1);
-            return false;
+        if ((i & 255) == 0) {
+            if (*err) return false;
+            if (clock64() - t0 > TC_TIMEOUT_CYCLES) {
+                atomicExch((int *)err, 1);
+                return false;
+            }
         }
     }
 }

@@ -57,12 +57,22 @@ def _rows_to_lists(idx: np.ndarray, dist: np.ndarray, cnt: np.ndarray, as_int: b
 class IVFFlatL2Index:
     """GPU IVF-flat over squared L2 (drop-in for pynear.IVFFlatL2Index)."""
 
-    def __init__(self, n_clusters: int = 100, n_probe: int = 10):
+    def __init__(self, n_clusters: int = 100, n_probe: int = 10, engine: str = "fp32", shortlist: int = 40):
+        """engine "fp32": CUDA-core scan with the reference's |q|^2+|x|^2-2q.x
+        distances; engine "tc": BF16 tensor-core shortlist of `shortlist`
+        candidates per query, re-ranked with exact FP32 squared L2 (k <= 32)."""
         self._n_clusters_req = int(n_clusters)
         self._n_probe = min(int(n_probe), int(n_clusters))
         self._h = _lib.Handle("gn_ivfl2_create", self._n_clusters_req, self._n_probe)
         self._built = False
         self._state = None  # host copy for pickling: (data, centroids, labels)
+        self.set_engine(engine, shortlist)
+
+    def set_engine(self, engine: str, shortlist: int = 40) -> None:
+        if engine not in ("fp32", "tc"):
+            raise ValueError('engine must be "fp32" or "tc"')
+        _lib.call("gn_ivfl2_set_mode", self._h.h, 0 if engine == "fp32" else 1, int(shortlist))
+        self._engine, self._shortlist = engine, int(shortlist)
 
     def set(self, data) -> None:
         arr = _f32_2d(data, "data")
@@ -135,7 +145,8 @@ class IVFFlatL2Index:
         return cent, offs, ids
 
     def __getstate__(self):
-        st = {"n_clusters": self._n_clusters_req, "n_probe": self._n_probe, "built": self._built}
+        st = {"n_clusters": self._n_clusters_req, "n_probe": self._n_probe, "built": self._built,
+              "engine": self._engine, "shortlist": self._shortlist}
         if self._built:
             cent, offs, ids = self.export()
             labels = np.empty(self._data.shape[0], np.int32)
@@ -145,7 +156,7 @@ class IVFFlatL2Index:
         return st
 
     def __setstate__(self, st):
-        self.__init__(st["n_clusters"], st["n_probe"])
+        self.__init__(st["n_clusters"], st["n_probe"], st.get("engine", "fp32"), st.get("shortlist", 40))
         if st["built"]:
             self.set_assigned(st["data"], st["centroids"], st["labels"])
 

@@ -39,3 +39,31 @@ def test_tc_small_batches_and_tiny_db(gn, oracle):
     idx, dist = tc.search_knn_arrays(q, 10)
     oi, od = oracle.knn_float("l2", db, q, 10)
     assert np.array_equal(idx, oi)
+
+
+def test_ivf_tc_engine_matches_exact_within_probed_lists(gn, oracle):
+    """Tensor-core IVF: same lists and probes as the FP32 engine; its top-k are
+    the exact top-k of the probed lists (FP64-checked distances)."""
+    rng = np.random.default_rng(41)
+    centres = rng.standard_normal((64, 256), dtype=np.float32)
+    w = 1.0 / np.arange(1, 65) ** 1.1
+    comp = rng.choice(64, size=40000, p=w / w.sum())
+    data = (centres[comp] + np.float32(0.3) * rng.standard_normal((40000, 256), dtype=np.float32))
+    q = (centres[rng.choice(64, 257, p=w / w.sum())] + np.float32(0.3) * rng.standard_normal((257, 256), dtype=np.float32))
+    ix = gn.IVFFlatL2Index(n_clusters=48, n_probe=5, engine="tc")
+    ix.set(data)
+    cent, offs, ids = ix.export()
+    labels = np.empty(len(data), np.int32)
+    for c in range(len(offs) - 1):
+        labels[ids[offs[c]:offs[c + 1]]] = c
+    idx, dist, cnt = ix.search_knn_arrays(q, 10)
+    oi, od, oc = oracle.ivfl2_search(data, cent, labels, q, 10, 5)
+    assert np.array_equal(cnt, oc)
+    assert np.mean(idx == oi) >= 0.995
+    np.testing.assert_allclose(dist, od, rtol=1e-4, atol=1e-3)
+    # exact distances: compare with an FP64 recomputation of the returned rows
+    d64 = ((q[:, None, :].astype(np.float64) - data[idx].astype(np.float64)) ** 2).sum(-1)
+    assert np.max(np.abs(dist - d64) / np.maximum(d64, 1e-6)) < 1e-6
+    ix.set_engine("fp32")
+    fi, fd, fc = ix.search_knn_arrays(q, 10)
+    assert np.mean(fi == idx) >= 0.995
