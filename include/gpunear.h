@@ -132,6 +132,10 @@ int gn_ivfl2_set_n_probe(gn_index *ix, int32_t n_probe);
 int gn_ivfl2_set_mode(gn_index *ix, int32_t mode, int32_t shortlist);
 /* error word of the last tensor-core launch (nonzero: a bounded wait expired) */
 int gn_ivfl2_error(gn_index *ix, int32_t *err_out);
+/* Work of the last search, for throughput accounting (no reference
+ * counterpart): out[0] (query, probe) pairs, out[1] scored (pair, row)
+ * entries, out[2] rows of the distinct lists probed, out[3] tensor-core units. */
+int gn_ivfl2_last_work(gn_index *ix, int64_t *out);
 int gn_ivfl2_info(gn_index *ix, int32_t *n_clusters_built, int32_t *n_probe, int64_t *n, int64_t *d);
 /* copy out the built state: centroids (n_clusters_built*d), list offsets
  * (n_clusters_built+1, int64), original ids in list order (n, int64) */

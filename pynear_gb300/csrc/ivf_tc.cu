@@ -258,3 +258,30 @@ extern "C" int gn_ivfl2_error(gn_index *ix, int32_t *err_out) {
     if (err_out) *err_out = herr;
     return GN_OK;
 }
+
+// Work of the last search (benchmark accounting; computed on demand):
+// out[0] (query, probe) pairs, out[1] scored (pair, row) entries, out[2] rows
+// of the distinct lists probed, out[3] tensor-core work units.
+extern "C" int gn_ivfl2_last_work(gn_index *ix, int64_t *out) {
+    if (!ix || ix->kind != K_IVFL2 || !ix->ivfl2) return fail(GN_ERR_INVALID, "not an IVFFlatL2 index");
+    IvfL2State &S = *ix->ivfl2;
+    IvfScratch &T = S.s;
+    std::lock_guard<std::mutex> lk(ix->mu);
+    if (!T.bcnt.p || S.nc == 0) return fail(GN_ERR_INVALID, "no search has run");
+    std::vector<int32_t> cnt((size_t)S.nc);
+    GN_CUDA_TRY(cudaMemcpy(cnt.data(), T.bcnt.p, (size_t)S.nc * 4, cudaMemcpyDeviceToHost));
+    int64_t pairs = 0, scored = 0, rows = 0;
+    for (int32_t l = 0; l < S.nc; ++l) {
+        const int64_t len = S.h_off[(size_t)l + 1] - S.h_off[(size_t)l];
+        pairs += cnt[(size_t)l];
+        scored += (int64_t)cnt[(size_t)l] * len;
+        if (cnt[(size_t)l] > 0) rows += len;
+    }
+    int64_t units = 0;
+    if (S.mode == 1 && S.nunits.p) GN_CUDA_TRY(cudaMemcpy(&units, S.nunits.p, 8, cudaMemcpyDeviceToHost));
+    out[0] = pairs;
+    out[1] = scored;
+    out[2] = rows;
+    out[3] = units;
+    return GN_OK;
+}
