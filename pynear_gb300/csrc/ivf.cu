@@ -38,15 +38,20 @@ constexpr int IVF_QCHUNK_L2 = GT_BM;  // queries per float work item
 constexpr int IVF_QCHUNK_BIN = 32;    // queries per binary work item (4 warps x 8)
 
 // ── coarse probing (float): GEMM + per-query top-nprobe ───────────────────
+// blockIdx.y selects a slice of cps centroids (one slice when the batch alone
+// fills the GPU); with several slices each writes its sorted partial top-np
+// keys to part[(q * gridDim.y + slice) * np ...] for coarse_merge_kernel.
 template <int R>
 __global__ void __launch_bounds__(GT_THREADS) ivf_coarse_kernel(const float *__restrict__ Q,
                                                                 const float *__restrict__ qn, int64_t nq, int dp,
                                                                 const float *__restrict__ C,
                                                                 const float *__restrict__ cn, int nc, int np,
-                                                                int32_t *__restrict__ probes) {
+                                                                int cps, int32_t *__restrict__ probes,
+                                                                uint64_t *__restrict__ part) {
     __shared__ GemmTileSmem s;
     __shared__ int64_t arow[GT_BM];
     const int64_t q0 = (int64_t)blockIdx.x * GT_BM;
+    const int cb = blockIdx.y * cps, ce = min(nc, cb + cps);
     if (threadIdx.x < GT_BM) arow[threadIdx.x] = (q0 + threadIdx.x < nq) ? q0 + threadIdx.x : -1;
     __syncthreads();
     const int tm = threadIdx.x >> 5, tn = threadIdx.x & 31;
@@ -55,8 +60,8 @@ __global__ void __launch_bounds__(GT_THREADS) ivf_coarse_kernel(const float *__r
 #pragma unroll
     for (int i = 0; i < 8; ++i) { L[i].init(); thr[i] = KEY_EMPTY; }
     float acc[8][4];
-    for (int c0 = 0; c0 < nc; c0 += GT_BN) {
-        gt_tile(s, acc, Q, arow, dp, C, c0, nc, dp, dp);
+    for (int c0 = cb; c0 < ce; c0 += GT_BN) {
+        gt_tile(s, acc, Q, arow, dp, C, c0, ce, dp, dp);
 #pragma unroll
         for (int i = 0; i < 8; ++i) {
             const int64_t q = arow[tm * 8 + i];
@@ -65,7 +70,7 @@ __global__ void __launch_bounds__(GT_THREADS) ivf_coarse_kernel(const float *__r
             for (int j = 0; j < 4; ++j) {
                 const int c = c0 + tn * 4 + j;
                 uint64_t key = KEY_EMPTY;
-                if (c < nc && q >= 0) {
+                if (c < ce && q >= 0) {
                     const float v = fmaxf(0.f, fmaf(-2.f, acc[i][j], qv + cn[c]));
                     key = make_key(__float_as_uint(v), (uint32_t)c);
                 }
@@ -81,8 +86,31 @@ __global__ void __launch_bounds__(GT_THREADS) ivf_coarse_kernel(const float *__r
 #pragma unroll
         for (int r = 0; r < R; ++r) {
             const int p = r * 32 + lane;
-            if (p < np) probes[q * np + p] = (L[i].v[r] == KEY_EMPTY) ? -1 : (int32_t)key_idx(L[i].v[r]);
+            if (p >= np) continue;
+            if (part) part[((size_t)q * gridDim.y + blockIdx.y) * np + p] = L[i].v[r];
+            else probes[q * np + p] = (L[i].v[r] == KEY_EMPTY) ? -1 : (int32_t)key_idx(L[i].v[r]);
         }
+    }
+}
+
+template <int R>
+__global__ void coarse_merge_kernel(const uint64_t *__restrict__ part, int nsplit, int np, int64_t nq,
+                                    int32_t *__restrict__ probes) {
+    const int lane = threadIdx.x & 31;
+    const int64_t q = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (q >= nq) return;
+    WarpTopK<R> L;
+    L.init();
+    uint64_t thr = KEY_EMPTY;
+    for (int sp = 0; sp < nsplit; ++sp)
+        for (int j0 = 0; j0 < np; j0 += 32) {
+            const int j = j0 + lane;
+            L.offer(j < np ? part[((size_t)q * nsplit + sp) * np + j] : KEY_EMPTY, thr, np);
+        }
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+        const int p = r * 32 + lane;
+        if (p < np) probes[q * np + p] = (L.v[r] == KEY_EMPTY) ? -1 : (int32_t)key_idx(L.v[r]);
     }
 }
 
@@ -566,10 +594,21 @@ int ivfl2_coarse(gn_index *ix, const float *dQ, int64_t nq, int np, cudaStream_t
     GN_TRY(T.qn.ensure((size_t)nq * 4));
     GN_TRY(T.probes.ensure((size_t)nq * np * 4));
     row_norms(dQ, nq, S.dp, T.qn.as<float>(), st);
+    // small batches: split the centroids over more CTAs and merge
+    const int64_t qblocks = ceil_div(nq, GT_BM);
+    int nsplit = 1;
+    while (qblocks * nsplit * 2 <= dev_info().num_sms && (int64_t)GT_BN * nsplit * 2 <= S.nc) nsplit *= 2;
+    const int cps = (int)round_up(ceil_div(S.nc, nsplit), GT_BN);
+    nsplit = (int)ceil_div(S.nc, cps);
+    if (nsplit > 1) GN_TRY(T.cpart.ensure((size_t)nq * nsplit * np * 8));
     return dispatch_r(np, [&](auto RC) {
         constexpr int R = decltype(RC)::value;
-        ivf_coarse_kernel<R><<<(unsigned)ceil_div(nq, GT_BM), GT_THREADS, 0, st>>>(
-            dQ, T.qn.as<float>(), nq, S.dp, S.cent.as<float>(), S.cnorm.as<float>(), S.nc, np, T.probes.as<int32_t>());
+        ivf_coarse_kernel<R><<<dim3((unsigned)qblocks, (unsigned)nsplit), GT_THREADS, 0, st>>>(
+            dQ, T.qn.as<float>(), nq, S.dp, S.cent.as<float>(), S.cnorm.as<float>(), S.nc, np, cps,
+            T.probes.as<int32_t>(), nsplit > 1 ? T.cpart.as<uint64_t>() : nullptr);
+        if (nsplit > 1)
+            coarse_merge_kernel<R><<<(unsigned)ceil_div(nq, 4), 128, 0, st>>>(T.cpart.as<uint64_t>(), nsplit, np, nq,
+                                                                              T.probes.as<int32_t>());
         return GN_OK;
     });
 }

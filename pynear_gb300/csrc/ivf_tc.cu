@@ -97,47 +97,75 @@ __device__ __forceinline__ float l2sq_compensated(const float *__restrict__ q, c
     return __fadd_rn(s, c);
 }
 
+// Selection over a query's score segments.  W warps share one query (W = 1
+// for large batches, up to 16 for small ones): warp w takes every W-th block
+// of 128 scores, keeps a register top-S, the partial lists meet in shared
+// memory and warp 0 merges them, re-ranks the S candidates exactly and writes
+// the k nearest.
 template <int RS>
 __global__ void ivf_tc_select_kernel(const float *__restrict__ scores, const int32_t *__restrict__ probes, int np,
                                      const int64_t *__restrict__ qseg, const int64_t *__restrict__ seg_rel,
                                      const int64_t *__restrict__ list_off, int S, const float *__restrict__ Q,
                                      const float *__restrict__ X, int d, int dp, const int32_t *__restrict__ ids,
-                                     int64_t nq, int k, int64_t *__restrict__ out_idx, float *__restrict__ out_dist,
-                                     int64_t *__restrict__ out_cnt) {
-    const int lane = threadIdx.x & 31;
-    const int64_t q = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-    if (q >= nq) return;
+                                     int64_t nq, int k, int W, int64_t *__restrict__ out_idx,
+                                     float *__restrict__ out_dist, int64_t *__restrict__ out_cnt) {
+    extern __shared__ uint64_t sel_smem[];  // [blockDim/32][32*RS] partial lists
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int qpb = (blockDim.x >> 5) / W;  // queries per block
+    const int64_t q = (int64_t)blockIdx.x * qpb + warp / W;
+    const int wq = warp % W;
+    const bool active = q < nq;
+    const float INF = __int_as_float(0x7f800000);
     WarpTopK<RS> L;
     L.init();
     uint64_t thr = KEY_EMPTY;
-    float thr_f = __int_as_float(0x7f800000);  // score of the S-th key (+inf until S are held)
-    const float INF = __int_as_float(0x7f800000);
-    for (int p = 0; p < np; ++p) {
-        const int64_t pair = q * np + p;
-        const int32_t l = probes[pair];
-        if (l < 0) continue;
-        const int64_t lb = list_off[l], len = list_off[l + 1] - lb;
-        const float *sc = scores + qseg[q] + seg_rel[pair];
-        for (int64_t i0 = 0; i0 < len; i0 += 128) {
-            // four independent loads in flight, then one vote rejects the
-            // whole 128-score block in the common case
-            float v[4];
+    float thr_f = INF;
+    if (active) {
+        int64_t blk = 0;  // running index of 128-score blocks over the query's segments
+        for (int p = 0; p < np; ++p) {
+            const int64_t pair = q * np + p;
+            const int32_t l = probes[pair];
+            if (l < 0) continue;
+            const int64_t lb = list_off[l], len = list_off[l + 1] - lb;
+            const float *sc = scores + qseg[q] + seg_rel[pair];
+            const int64_t nblk = (len + 127) / 128;
+            // first block of this segment owned by warp wq
+            int64_t b0 = (wq - blk % W + W) % W;
+            for (int64_t b = b0; b < nblk; b += W) {
+                const int64_t i0 = b * 128;
+                float v[4];
 #pragma unroll
-            for (int u = 0; u < 4; ++u) {
-                const int64_t i = i0 + u * 32 + lane;
-                v[u] = (i < len) ? __ldg(sc + i) : INF;
+                for (int u = 0; u < 4; ++u) {
+                    const int64_t i = i0 + u * 32 + lane;
+                    v[u] = (i < len) ? __ldg(sc + i) : INF;
+                }
+                const float m = fminf(fminf(v[0], v[1]), fminf(v[2], v[3]));
+                if (!__any_sync(0xffffffffu, m <= thr_f)) continue;
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const int64_t i = i0 + u * 32 + lane;
+                    const uint64_t key = (i < len) ? make_key(f2ord(v[u]), (uint32_t)(lb + i)) : KEY_EMPTY;
+                    L.offer(key, thr, S);
+                    thr_f = (thr == KEY_EMPTY) ? INF : ord2f(key_dist(thr));
+                }
             }
-            const float m = fminf(fminf(v[0], v[1]), fminf(v[2], v[3]));
-            if (!__any_sync(0xffffffffu, m <= thr_f)) continue;
+            blk += nblk;
+        }
+    }
+    if (W > 1) {
+        uint64_t *mine = sel_smem + (size_t)warp * 32 * RS;
 #pragma unroll
-            for (int u = 0; u < 4; ++u) {
-                const int64_t i = i0 + u * 32 + lane;
-                const uint64_t key = (i < len) ? make_key(f2ord(v[u]), (uint32_t)(lb + i)) : KEY_EMPTY;
-                L.offer(key, thr, S);
-                thr_f = (thr == KEY_EMPTY) ? INF : ord2f(key_dist(thr));
+        for (int r = 0; r < RS; ++r) mine[r * 32 + lane] = L.v[r];
+        __syncthreads();
+        if (wq == 0 && active) {
+            for (int w = 1; w < W; ++w) {
+                const uint64_t *other = sel_smem + (size_t)(warp + w) * 32 * RS;
+#pragma unroll
+                for (int r = 0; r < RS; ++r) L.offer(other[r * 32 + lane], thr, S);
             }
         }
     }
+    if (!active || wq != 0) return;
     WarpTopK<1> F;
     F.init();
     uint64_t fthr = KEY_EMPTY;
@@ -184,8 +212,10 @@ int ivfl2_search_tc(gn_index *ix, const float *dQ, int64_t nq, int k, int64_t *d
     if (S.K == 0) GN_TRY(ivfl2_prepare_tc(ix, st));
     const int np = std::min<int32_t>(S.nprobe, S.nc);
     GN_TRY(ivfl2_coarse(ix, dQ, nq, np, st));
-    // work items of rc_tc rows; every pair owns a score segment (slot_rc = 1)
-    GN_TRY(ivf_plan(T, nq, np, S.nc, S.list_off.as<int64_t>(), S.rc_tc, TC_QCHUNK, st, 1));
+    // work items of rc rows (short items for small batches so that their few
+    // lists still spread over all SMs); every pair owns a score segment
+    const int rc = nq >= 512 ? S.rc_tc : (nq >= 64 ? 1024 : 256);
+    GN_TRY(ivf_plan(T, nq, np, S.nc, S.list_off.as<int64_t>(), rc, TC_QCHUNK, st, 1));
     const int64_t npairs = nq * np;
     const int64_t qb_rows = std::max<int64_t>(npairs, TC_QCHUNK);
     GN_TRY(S.qb.ensure((size_t)qb_rows * S.K * 2));
@@ -195,11 +225,11 @@ int ivfl2_search_tc(gn_index *ix, const float *dQ, int64_t nq, int k, int64_t *d
                                                      T.slot_rel.as<int64_t>(), S.qb.as<__nv_bfloat16>(),
                                                      S.aslot.as<int64_t>(), npairs);
     const int64_t maxlen = S.top_rows.size() > 1 ? S.top_rows[1] : 0;
-    const int64_t max_units = (ceil_div(npairs, TC_QCHUNK) + S.nc) * (ceil_div(maxlen, S.rc_tc) + 1);
+    const int64_t max_units = (ceil_div(npairs, TC_QCHUNK) + S.nc) * (ceil_div(maxlen, rc) + 1);
     GN_TRY(S.units.ensure((size_t)max_units * sizeof(TcUnit)));
     GN_TRY(S.nunits.ensure(8));
     tc_units_kernel<<<(unsigned)ceil_div(max_units, 256), 256, 0, st>>>(
-        T.item_off.as<int64_t>(), S.nc, T.boff.as<int64_t>(), S.list_off.as<int64_t>(), S.rc_tc, max_units,
+        T.item_off.as<int64_t>(), S.nc, T.boff.as<int64_t>(), S.list_off.as<int64_t>(), rc, max_units,
         S.units.as<TcUnit>(), S.nunits.as<int64_t>());
     // score segments: at most the rows of the np largest lists per query
     const int64_t seg_total = nq * S.top_rows[(size_t)std::min<int64_t>(np, (int64_t)S.top_rows.size() - 1)];
@@ -222,13 +252,19 @@ int ivfl2_search_tc(gn_index *ix, const float *dQ, int64_t nq, int k, int64_t *d
     timing_begin(st, "tc_topk_kernel<store>");
     GN_TRY(tc_topk_launch(a, st));
     timing_end(st);
-    const unsigned blocks = (unsigned)ceil_div(nq, 4);
+    // warps per query: enough warps in flight for small batches
+    int W = 1;
+    while (W < 16 && nq * W * 2 <= (int64_t)dev_info().num_sms * 32) W *= 2;
+    const int qpb = std::max(1, 8 / W);
+    const int threads = 32 * W * qpb;
+    const unsigned blocks = (unsigned)ceil_div(nq, qpb);
     auto sel = [&](auto RC) {
         constexpr int R = decltype(RC)::value;
-        ivf_tc_select_kernel<R><<<blocks, 128, 0, st>>>(S.scores.as<float>(), T.probes.as<int32_t>(), np,
-                                                       T.qslot.as<int64_t>(), T.slot_rel.as<int64_t>(),
-                                                       S.list_off.as<int64_t>(), S.shortlist, dQ, S.vecs.as<float>(),
-                                                       S.d, S.dp, S.ids.as<int32_t>(), nq, k, d_idx, d_dist, d_cnt);
+        const size_t smem = W > 1 ? (size_t)(threads / 32) * 32 * R * 8 : 0;
+        ivf_tc_select_kernel<R><<<blocks, threads, smem, st>>>(
+            S.scores.as<float>(), T.probes.as<int32_t>(), np, T.qslot.as<int64_t>(), T.slot_rel.as<int64_t>(),
+            S.list_off.as<int64_t>(), S.shortlist, dQ, S.vecs.as<float>(), S.d, S.dp, S.ids.as<int32_t>(), nq, k, W,
+            d_idx, d_dist, d_cnt);
     };
     if (S.shortlist <= 32) sel(std::integral_constant<int, 1>());
     else sel(std::integral_constant<int, 2>());
