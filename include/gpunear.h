@@ -141,6 +141,31 @@ int gn_ivfl2_info(gn_index *ix, int32_t *n_clusters_built, int32_t *n_probe, int
  * (n_clusters_built+1, int64), original ids in list order (n, int64) */
 int gn_ivfl2_export(gn_index *ix, float *centroids, int64_t *offsets, int64_t *ids);
 
+/* ── learned probing (no reference counterpart) ───────────────────────────
+ * An MLP (64 -> 256 -> 256 -> one logit per list; BF16 weights, FP32
+ * accumulation at inference) scores a query's 64 nearest lists by the
+ * probability that they hold one of its exact 10 nearest neighbours; the index
+ * probes the lists whose logit reaches a threshold (always the nearest one),
+ * instead of a fixed n_probe.  Trained on the GPU by the library's own forward,
+ * backward and Adam kernels against labels from exact search.
+ * Parameters are one flat FP32 array: W1 [nlist x 256] | b1 [256] |
+ * W2 [256 x 256] | b2 [256] | W3 [nlist x 256] | b3 [nlist].
+ */
+int gn_prober_create(int32_t nlist, uint32_t seed, gn_index **out);
+int gn_prober_num_params(gn_index *pr, int64_t *n);
+int gn_prober_get_params(gn_index *pr, float *out);
+int gn_prober_set_params(gn_index *pr, const float *in);
+/* mean binary cross-entropy and its gradient for B explicit examples:
+ * cand [B x 64] list ids (-1 = none), feat [B x 64], lab [B x 64] in {0,1} */
+int gn_prober_loss_grad(gn_index *pr, int64_t B, const int32_t *cand, const float *feat, const float *lab,
+                        float *loss_out, float *grads_out);
+/* queries: nq host rows of the index dimension; gt: [nq x k] exact neighbour
+ * ids; loss_out: one mean loss per epoch */
+int gn_prober_train(gn_index *pr, gn_index *ivf, const float *queries, int64_t nq, const int64_t *gt, int32_t k,
+                    int32_t epochs, int32_t batch, float lr, float *loss_out);
+int gn_ivfl2_set_prober(gn_index *ivf, gn_index *pr, float logit_tau);
+int gn_ivfl2_last_nprobed(gn_index *ivf, int64_t nq, int32_t *out);
+
 /* ── IVF-flat binary index ────────────────────────────────────────────────
  * Replaces IVFFlatBinaryIndex (pynear/include/BinaryIVF.hpp:34-227, bound at
  * pynear/src/PythonBindings.cpp:454-466): binary k-means++ and majority-vote

@@ -65,6 +65,14 @@ SIGNATURES = {
     "gn_ivfl2_last_work": [P, P],
     "gn_ivfl2_info": [P, P, P, P, P],
     "gn_ivfl2_export": [P, P, P, P],
+    "gn_prober_create": [I32, U32, PP],
+    "gn_prober_num_params": [P, P],
+    "gn_prober_get_params": [P, P],
+    "gn_prober_set_params": [P, P],
+    "gn_prober_loss_grad": [P, I64, P, P, P, P, P],
+    "gn_prober_train": [P, P, P, I64, P, I32, I32, I32, ctypes.c_float, P],
+    "gn_ivfl2_set_prober": [P, P, ctypes.c_float],
+    "gn_ivfl2_last_nprobed": [P, I64, P],
     "gn_ivfbin_create": [I32, I32, I32, U32, PP],
     "gn_ivfbin_set": [P, P, I64, I64],
     "gn_ivfbin_search_knn": [P, P, I64, I64, P, P, P],

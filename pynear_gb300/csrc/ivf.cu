@@ -29,6 +29,7 @@
 #include "gemm_topk.cuh"
 #include "ivf.cuh"
 #include "kmeans.cuh"
+#include "prober.cuh"
 #include "timing.cuh"
 #include "topk.cuh"
 
@@ -95,7 +96,7 @@ __global__ void __launch_bounds__(GT_THREADS) ivf_coarse_kernel(const float *__r
 
 template <int R>
 __global__ void coarse_merge_kernel(const uint64_t *__restrict__ part, int nsplit, int np, int64_t nq,
-                                    int32_t *__restrict__ probes) {
+                                    int32_t *__restrict__ probes, uint64_t *__restrict__ keys_out) {
     const int lane = threadIdx.x & 31;
     const int64_t q = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     if (q >= nq) return;
@@ -110,7 +111,9 @@ __global__ void coarse_merge_kernel(const uint64_t *__restrict__ part, int nspli
 #pragma unroll
     for (int r = 0; r < R; ++r) {
         const int p = r * 32 + lane;
-        if (p < np) probes[q * np + p] = (L.v[r] == KEY_EMPTY) ? -1 : (int32_t)key_idx(L.v[r]);
+        if (p >= np) continue;
+        if (keys_out) keys_out[q * np + p] = L.v[r];
+        else probes[q * np + p] = (L.v[r] == KEY_EMPTY) ? -1 : (int32_t)key_idx(L.v[r]);
     }
 }
 
@@ -587,33 +590,75 @@ static int ivfl2_build_from_labels(gn_index *ix, const float *dX, int64_t n, int
     return GN_OK;
 }
 
-// Coarse probing of a float IVF: qn = |q|^2, probes = the np nearest lists.
-int ivfl2_coarse(gn_index *ix, const float *dQ, int64_t nq, int np, cudaStream_t st) {
+// Coarse probing of a float IVF: qn = |q|^2 and the np nearest lists of each
+// query.  Small batches split the centroids over more CTAs.  With keep_keys
+// the sorted partial key lists stay in T.cpart (nsplit of them per query) and
+// probes are not written; otherwise probes get the merged list ids.
+int ivfl2_coarse_run(gn_index *ix, const float *dQ, int64_t nq, int np, bool keep_keys, int *nsplit_out,
+                     cudaStream_t st) {
     IvfL2State &S = *ix->ivfl2;
     IvfScratch &T = S.s;
     GN_TRY(T.qn.ensure((size_t)nq * 4));
     GN_TRY(T.probes.ensure((size_t)nq * np * 4));
     row_norms(dQ, nq, S.dp, T.qn.as<float>(), st);
-    // small batches: split the centroids over more CTAs and merge
     const int64_t qblocks = ceil_div(nq, GT_BM);
     int nsplit = 1;
     while (qblocks * nsplit * 2 <= dev_info().num_sms && (int64_t)GT_BN * nsplit * 2 <= S.nc) nsplit *= 2;
     const int cps = (int)round_up(ceil_div(S.nc, nsplit), GT_BN);
     nsplit = (int)ceil_div(S.nc, cps);
-    if (nsplit > 1) GN_TRY(T.cpart.ensure((size_t)nq * nsplit * np * 8));
+    const bool use_part = keep_keys || nsplit > 1;
+    if (use_part) GN_TRY(T.cpart.ensure((size_t)nq * nsplit * np * 8));
+    if (nsplit_out) *nsplit_out = nsplit;
     return dispatch_r(np, [&](auto RC) {
         constexpr int R = decltype(RC)::value;
         ivf_coarse_kernel<R><<<dim3((unsigned)qblocks, (unsigned)nsplit), GT_THREADS, 0, st>>>(
             dQ, T.qn.as<float>(), nq, S.dp, S.cent.as<float>(), S.cnorm.as<float>(), S.nc, np, cps,
-            T.probes.as<int32_t>(), nsplit > 1 ? T.cpart.as<uint64_t>() : nullptr);
-        if (nsplit > 1)
+            T.probes.as<int32_t>(), use_part ? T.cpart.as<uint64_t>() : nullptr);
+        if (use_part && !keep_keys)
             coarse_merge_kernel<R><<<(unsigned)ceil_div(nq, 4), 128, 0, st>>>(T.cpart.as<uint64_t>(), nsplit, np, nq,
-                                                                              T.probes.as<int32_t>());
+                                                                              T.probes.as<int32_t>(), nullptr);
         return GN_OK;
     });
 }
 
+int ivfl2_coarse(gn_index *ix, const float *dQ, int64_t nq, int np, cudaStream_t st) {
+    return ivfl2_coarse_run(ix, dQ, nq, np, false, nullptr, st);
+}
+
+// The np nearest lists of each query as sorted keys (squared distance, list).
+int ivfl2_coarse_sorted_keys(gn_index *ix, const float *dQ, int64_t nq, int np, uint64_t *keys, cudaStream_t st) {
+    int nsplit = 1;
+    GN_TRY(ivfl2_coarse_run(ix, dQ, nq, np, true, &nsplit, st));
+    IvfScratch &T = ix->ivfl2->s;
+    return dispatch_r(np, [&](auto RC) {
+        constexpr int R = decltype(RC)::value;
+        coarse_merge_kernel<R><<<(unsigned)ceil_div(nq, 4), 128, 0, st>>>(T.cpart.as<uint64_t>(), nsplit, np, nq,
+                                                                          nullptr, keys);
+        return GN_OK;
+    });
+}
+
+// Probes of a batch: the learned prober when one is attached (up to 64 lists,
+// -1 padded), else the fixed n_probe nearest lists.  Returns the probe width.
+int ivfl2_probes(gn_index *ix, const float *dQ, int64_t nq, int *np_out, cudaStream_t st) {
+    IvfL2State &S = *ix->ivfl2;
+    if (S.prober) {
+        if (S.nc < PROBER_CAND) return fail(GN_ERR_INVALID, "learned probing needs at least 64 lists");
+        GN_TRY(S.s.nprobed.ensure((size_t)nq * 4));
+        GN_TRY(prober_apply(S.prober, ix, dQ, nq, S.prober_tau, S.s.probes.as<int32_t>(), S.s.nprobed.as<int32_t>(),
+                            st));
+        *np_out = PROBER_CAND;
+        return GN_OK;
+    }
+    const int np = std::min<int32_t>(S.nprobe, S.nc);
+    *np_out = np;
+    return ivfl2_coarse(ix, dQ, nq, np, st);
+}
+
 // ── float IVF: search on device buffers ───────────────────────────────────
+static int ivfl2_scan_fp32(gn_index *ix, const float *dQ, int64_t nq, int np, int k, int64_t *d_idx, float *d_dist,
+                           int64_t *d_cnt, cudaStream_t st);
+
 static int ivfl2_search_dev(gn_index *ix, const float *dQ, int64_t nq, int k, int64_t *d_idx, float *d_dist,
                             int64_t *d_cnt, cudaStream_t st) {
     IvfL2State &S = *ix->ivfl2;
@@ -623,7 +668,15 @@ static int ivfl2_search_dev(gn_index *ix, const float *dQ, int64_t nq, int k, in
     if (np > 256) return fail(GN_ERR_UNSUPPORTED, "n_probe > 256 is not supported");
     if (nq == 0) return GN_OK;
     if (S.mode == 1) return ivfl2_search_tc(ix, dQ, nq, k, d_idx, d_dist, d_cnt, st);
-    GN_TRY(ivfl2_coarse(ix, dQ, nq, np, st));
+    int npw = np;
+    GN_TRY(ivfl2_probes(ix, dQ, nq, &npw, st));
+    return ivfl2_scan_fp32(ix, dQ, nq, npw, k, d_idx, d_dist, d_cnt, st);
+}
+
+static int ivfl2_scan_fp32(gn_index *ix, const float *dQ, int64_t nq, int np, int k, int64_t *d_idx, float *d_dist,
+                           int64_t *d_cnt, cudaStream_t st) {
+    IvfL2State &S = *ix->ivfl2;
+    IvfScratch &T = S.s;
     const int64_t slots = nq * max_slots_per_query(S.top_rows, np, S.rc);
     GN_TRY(T.part.ensure((size_t)slots * k * 8));
     if (!g_scan_blocks_l2) {

@@ -10,7 +10,7 @@ namespace gn {
 // Per-batch scratch of an IVF search (device resident, reused).
 struct IvfScratch {
     DBuf q, qn, probes, probes64, pdist, bcnt, boff, bucket, fill, slot_rel, qcount, qslot, item_off, counter, part,
-        cpart;
+        cpart, nprobed;
 };
 
 // Float IVF (forest.py IVFFlatL2Index semantics, squared L2).
@@ -33,6 +33,9 @@ struct IvfL2State {
     int rc_tc = 4096;            // list rows per tensor-core work unit
     DBuf x16;                    // n*K BF16 rows, list order
     DBuf qb, aslot, units, nunits, err, scores;
+    // learned probing (prober.cu): attached model and logit threshold
+    gn_index *prober = nullptr;
+    float prober_tau = 0.f;
 };
 
 // Binary IVF (IVFFlatBinaryIndex semantics).
@@ -58,6 +61,10 @@ int ivf_plan(IvfScratch &S, int64_t nq, int np, int nc, const int64_t *d_list_of
              cudaStream_t st, int slot_rc = 0);
 int64_t ivf_max_slots_per_query(const std::vector<int64_t> &top, int np, int rc);
 int ivfl2_coarse(gn_index *ix, const float *dQ, int64_t nq, int np, cudaStream_t st);
+int ivfl2_coarse_run(gn_index *ix, const float *dQ, int64_t nq, int np, bool keep_keys, int *nsplit_out,
+                     cudaStream_t st);
+int ivfl2_coarse_sorted_keys(gn_index *ix, const float *dQ, int64_t nq, int np, uint64_t *keys, cudaStream_t st);
+int ivfl2_probes(gn_index *ix, const float *dQ, int64_t nq, int *np_out, cudaStream_t st);
 int ivfl2_search_tc(gn_index *ix, const float *dQ, int64_t nq, int k, int64_t *d_idx, float *d_dist, int64_t *d_cnt,
                     cudaStream_t st);
 int ivfl2_prepare_tc(gn_index *ix, cudaStream_t st);

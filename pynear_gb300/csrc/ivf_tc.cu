@@ -210,8 +210,8 @@ int ivfl2_search_tc(gn_index *ix, const float *dQ, int64_t nq, int k, int64_t *d
     IvfScratch &T = S.s;
     if (k > 32 || k > S.shortlist) return fail(GN_ERR_UNSUPPORTED, "tensor-core IVF supports k <= min(32, shortlist)");
     if (S.K == 0) GN_TRY(ivfl2_prepare_tc(ix, st));
-    const int np = std::min<int32_t>(S.nprobe, S.nc);
-    GN_TRY(ivfl2_coarse(ix, dQ, nq, np, st));
+    int np = 1;
+    GN_TRY(ivfl2_probes(ix, dQ, nq, &np, st));
     // work items of rc rows (short items for small batches so that their few
     // lists still spread over all SMs); every pair owns a score segment
     const int rc = nq >= 512 ? S.rc_tc : (nq >= 64 ? 1024 : 256);

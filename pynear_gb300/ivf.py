@@ -82,6 +82,20 @@ class IVFFlatL2Index:
         self._state = None
         self._data = arr
 
+    def set_prober(self, prober, threshold: float = 0.5) -> None:
+        """Probe adaptively with a trained LearnedProber (probability threshold),
+        or with prober=None go back to the fixed n_probe."""
+        from .prober import prob_to_logit
+        self._prober = prober  # keeps the model alive while attached
+        _lib.call("gn_ivfl2_set_prober", self._h.h, None if prober is None else prober._h.h,
+                  prob_to_logit(threshold))
+
+    def last_lists_probed(self, nq: int) -> np.ndarray:
+        """Lists probed per query by the last search with a prober."""
+        out = np.empty(nq, np.int32)
+        _lib.call("gn_ivfl2_last_nprobed", self._h.h, nq, _lib.ptr(out))
+        return out
+
     def set_assigned(self, data, centroids, labels) -> None:
         """Build the lists from given centroids and labels (no k-means)."""
         arr = _f32_2d(data, "data")
