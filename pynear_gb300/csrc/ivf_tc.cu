@@ -4,11 +4,10 @@
 //   1. Qb      the BF16 copy of each (query, probe) pair's query, rows grouped by
 //              list (bucket order), so one TMA box covers a work unit's queries;
 //   2. units   one tensor-core work unit per (list, 128-query chunk, row chunk);
-//   3. scan    tc_topk_kernel in store mode: BF16 tcgen05 GEMM of the unit's
-//              queries against the list's BF16 rows with FP32 accumulation;
-//              the score |x|^2 - 2 q.x (exact FP32 |x|^2) of every (pair, row)
-//              goes to the pair's segment of a score buffer (coalesced stores
-//              through a shared-memory transpose);
+//   3. scan    tc_ivf_kernel: BF16 tcgen05 GEMM of the list's rows (M = 128
+//              per tile) against the unit's queries (N = 32..256) with FP32
+//              accumulation; the score |x|^2 - 2 q.x (exact FP32 |x|^2) of
+//              every (pair, row) goes to the pair's segment of a score buffer;
 //   4. select  one warp per query walks its probed lists' segments with a
 //              register top-S (S = shortlist), recomputes the S candidates'
 //              squared L2 exactly in FP32 with a compensated sum (two-product
@@ -25,6 +24,7 @@
 
 #include "ivf.cuh"
 #include "kmeans.cuh"
+#include "tc_ivf.cuh"
 #include "tc_scan.cuh"
 #include "timing.cuh"
 #include "gemm_topk.cuh"
@@ -32,7 +32,7 @@
 
 namespace gn {
 
-constexpr int TC_QCHUNK = 128;
+constexpr int TC_QCHUNK = 256;  // queries per tensor-core work unit (MMA N <= 256)
 
 __global__ void qb_fill_kernel(const float *__restrict__ Q, int d, int dp, int K, int np,
                                const int64_t *__restrict__ bucket, const int64_t *__restrict__ boff_end,
@@ -217,7 +217,7 @@ int ivfl2_search_tc(gn_index *ix, const float *dQ, int64_t nq, int k, int64_t *d
     const int rc = nq >= 512 ? S.rc_tc : (nq >= 64 ? 1024 : 256);
     GN_TRY(ivf_plan(T, nq, np, S.nc, S.list_off.as<int64_t>(), rc, TC_QCHUNK, st, 1));
     const int64_t npairs = nq * np;
-    const int64_t qb_rows = std::max<int64_t>(npairs, TC_QCHUNK);
+    const int64_t qb_rows = std::max<int64_t>(npairs, 256);  // >= one 256-row TMA box
     GN_TRY(S.qb.ensure((size_t)qb_rows * S.K * 2));
     GN_TRY(S.aslot.ensure((size_t)npairs * 8));
     qb_fill_kernel<<<(unsigned)npairs, 128, 0, st>>>(dQ, S.d, S.dp, S.K, np, T.bucket.as<int64_t>(),
@@ -234,23 +234,21 @@ int ivfl2_search_tc(gn_index *ix, const float *dQ, int64_t nq, int k, int64_t *d
     // score segments: at most the rows of the np largest lists per query
     const int64_t seg_total = nq * S.top_rows[(size_t)std::min<int64_t>(np, (int64_t)S.top_rows.size() - 1)];
     GN_TRY(S.scores.ensure((size_t)std::max<int64_t>(seg_total, 1) * 4));
-    TcLaunch a;
-    a.A = S.qb.p;
-    a.a_rows = qb_rows;
-    a.B = S.x16.p;
-    a.b_rows = std::max<int64_t>(S.n, 256);
+    TcIvfLaunch a;
+    a.X = S.x16.p;
+    a.x_rows = std::max<int64_t>(S.n, 256);
+    a.Q = S.qb.p;
+    a.q_rows = qb_rows;
     a.K = S.K;
     a.units = S.units.as<TcUnit>();
     a.n_units = S.nunits.as<int64_t>();
-    a.cta_off = nullptr;
-    a.bnorm = S.vnorm.as<float>();
-    a.arow_slot = S.aslot.as<int64_t>();
+    a.xnorm = S.vnorm.as<float>();
+    a.aslot = S.aslot.as<int64_t>();
     a.scores = S.scores.as<float>();
     a.err = S.err.as<int>();
-    a.S = 0;  // store mode
     a.grid = dev_info().num_sms;
-    timing_begin(st, "tc_topk_kernel<store>");
-    GN_TRY(tc_topk_launch(a, st));
+    timing_begin(st, "tc_ivf_kernel");
+    GN_TRY(tc_ivf_launch(a, st));
     timing_end(st);
     // warps per query: enough warps in flight for small batches
     int W = 1;

@@ -1,0 +1,225 @@
+// tc_ivf.cu — tensor-core list scan of the float IVF index (store mode).
+//
+// Orientation: the list rows are the MMA's M side (128 rows per tile, one per
+// TMEM lane) and the queries probing the list are the N side, N = 32, 64, 128
+// or 256 (the smallest that holds the work unit's queries), so the MMA work
+// follows the number of queries actually probing the list.  One persistent CTA
+// per SM walks the work units (list, chunk of <= 256 queries, chunk of rows):
+//   warp 0     TMA: per 64-wide K slice, 128 list rows (BF16) and the unit's
+//              N query rows (BF16, bucket order) into a 3-stage ring;
+//   warp 1     TMEM (2 x 256 columns) and tcgen05.mma M=128, N, K=16;
+//   warps 2-9  epilogue: thread = list row; for each query column its score
+//              |x|^2 - 2 q.x (exact FP32 |x|^2) goes to that (query, probe)
+//              pair's segment at the row's offset — 32 lanes write 32
+//              consecutive rows, so every store is one 128-byte line.
+#include <cuda_bf16.h>
+
+#include <algorithm>
+
+#include "index.cuh"
+#include "tc_ivf.cuh"
+#include "tc_sm100.cuh"
+
+namespace gn {
+
+constexpr int TI_M = 128, TI_NMAX = 256, TI_BK = 64, TI_STAGES = 3;
+constexpr int TI_A_BYTES = TI_M * TI_BK * 2;       // 16 KB
+constexpr int TI_B_BYTES = TI_NMAX * TI_BK * 2;    // 32 KB (max)
+constexpr int TI_STAGE_BYTES = TI_A_BYTES + TI_B_BYTES;
+constexpr int TI_NEPI = 8;
+constexpr int TI_THREADS = 64 + 32 * TI_NEPI;
+constexpr size_t TI_SMEM = 1024 + (size_t)TI_STAGES * TI_STAGE_BYTES + 256;
+
+__device__ __forceinline__ int ti_nsel(int na) { return na <= 32 ? 32 : na <= 64 ? 64 : na <= 128 ? 128 : 256; }
+
+__global__ void __launch_bounds__(TI_THREADS, 1)
+    tc_ivf_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constant__ CUtensorMap tmQ32,
+                  const __grid_constant__ CUtensorMap tmQ64, const __grid_constant__ CUtensorMap tmQ128,
+                  const __grid_constant__ CUtensorMap tmQ256, const TcUnit *__restrict__ units,
+                  const int64_t *__restrict__ n_units_ptr, int K, const float *__restrict__ xnorm,
+                  const int64_t *__restrict__ aslot, float *__restrict__ scores, int *__restrict__ err) {
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
+    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + TI_STAGES * TI_STAGE_BYTES);
+    uint64_t *full = bars, *empty = bars + TI_STAGES, *accfull = bars + 2 * TI_STAGES,
+             *accempty = bars + 2 * TI_STAGES + 2;
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 2 * TI_STAGES + 4);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    volatile int *verr = err;
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < TI_STAGES; ++s) {
+            mbar_init(full + s, 1);
+            mbar_init(empty + s, 1);
+        }
+        for (int b = 0; b < 2; ++b) {
+            mbar_init(accfull + b, 1);
+            mbar_init(accempty + b, TI_NEPI);
+        }
+        mbar_fence_init();
+    }
+    if (warp == 1) tmem_alloc(tmem_slot, 512);
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
+    const int64_t n_units = *n_units_ptr;
+    const int nk = K / TI_BK;
+
+    if (warp == 0) {
+        if (lane == 0) {
+            uint32_t it = 0;
+            bool ok = true;
+            for (int64_t u = blockIdx.x; u < n_units && ok; u += gridDim.x) {
+                const TcUnit un = units[u];
+                const int nsel = ti_nsel(un.na);
+                const CUtensorMap *mq = nsel == 32 ? &tmQ32 : nsel == 64 ? &tmQ64 : nsel == 128 ? &tmQ128 : &tmQ256;
+                const uint32_t bytes = TI_A_BYTES + (uint32_t)nsel * TI_BK * 2;
+                const int ntile = (int)((un.r1 - un.r0 + TI_M - 1) / TI_M);
+                for (int t = 0; t < ntile && ok; ++t)
+                    for (int kb = 0; kb < nk; ++kb, ++it) {
+                        const int s = it % TI_STAGES;
+                        const uint32_t ph = (it / TI_STAGES) & 1;
+                        if (!mbar_wait(empty + s, ph ^ 1, verr)) { ok = false; break; }
+                        uint8_t *sa = smem + s * TI_STAGE_BYTES;
+                        mbar_expect_tx(full + s, bytes);
+                        tma_load_2d(sa, &tmX, kb * TI_BK, (int)(un.r0 + (int64_t)t * TI_M), full + s);
+                        tma_load_2d(sa + TI_A_BYTES, mq, kb * TI_BK, (int)un.a0, full + s);
+                    }
+            }
+        }
+    } else if (warp == 1) {
+        if (lane == 0) {
+            uint32_t it = 0, tile_it = 0;
+            bool ok = true;
+            for (int64_t u = blockIdx.x; u < n_units && ok; u += gridDim.x) {
+                const TcUnit un = units[u];
+                const int nsel = ti_nsel(un.na);
+                const uint32_t idesc = idesc_bf16_f32(TI_M, nsel);
+                const int ntile = (int)((un.r1 - un.r0 + TI_M - 1) / TI_M);
+                for (int t = 0; t < ntile && ok; ++t, ++tile_it) {
+                    const int b = tile_it & 1;
+                    const uint32_t tph = (tile_it >> 1) & 1;
+                    if (!mbar_wait(accempty + b, tph ^ 1, verr)) { ok = false; break; }
+                    tc_fence_after();
+                    const uint32_t dt = tmem + (uint32_t)(b * TI_NMAX);
+                    for (int kb = 0; kb < nk; ++kb, ++it) {
+                        const int s = it % TI_STAGES;
+                        const uint32_t ph = (it / TI_STAGES) & 1;
+                        if (!mbar_wait(full + s, ph, verr)) { ok = false; break; }
+                        tc_fence_after();
+                        const uint32_t sa = smem_u32(smem + s * TI_STAGE_BYTES);
+                        const uint64_t da = sdesc_sw128(sa), db = sdesc_sw128(sa + TI_A_BYTES);
+#pragma unroll
+                        for (int kk = 0; kk < TI_BK / 16; ++kk)
+                            umma_bf16(dt, da + 2 * kk, db + 2 * kk, idesc, (kb | kk) ? 1u : 0u);
+                        umma_commit(empty + s);
+                    }
+                    if (ok) umma_commit(accfull + b);
+                }
+            }
+        }
+    } else {
+        const int quad = warp & 3;
+        const int grp = (warp - 2) >> 2;  // column chunks grp, grp + 2, ...
+        uint32_t tile_it = 0;
+        bool ok = true;
+        for (int64_t u = blockIdx.x; u < n_units && ok; u += gridDim.x) {
+            const TcUnit un = units[u];
+            const int nsel = ti_nsel(un.na);
+            const int nchunk = nsel / 32;
+            // segment base (minus the list start) of query column c*32 + lane
+            int64_t segv[TI_NMAX / 32 / 2];
+#pragma unroll
+            for (int cc = 0; cc < TI_NMAX / 32 / 2; ++cc) {
+                const int col = (grp + 2 * cc) * 32 + lane;
+                segv[cc] = (col < un.na) ? aslot[un.a0 + col] - un.rbase : INT64_MIN;
+            }
+            const int ntile = (int)((un.r1 - un.r0 + TI_M - 1) / TI_M);
+            for (int t = 0; t < ntile; ++t, ++tile_it) {
+                const int b = tile_it & 1;
+                const uint32_t tph = (tile_it >> 1) & 1;
+                const int64_t row = un.r0 + (int64_t)t * TI_M + quad * 32 + lane;
+                const bool rok = row < un.r1;
+                const float xn = rok ? __ldg(xnorm + row) : 0.f;
+                if (!mbar_wait(accfull + b, tph, verr)) { ok = false; break; }
+                tc_fence_after();
+#pragma unroll 1
+                for (int cc = 0; grp + 2 * cc < nchunk; ++cc) {
+                    const int c = grp + 2 * cc;
+                    float acc[32];
+                    tmem_ld32(tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(b * TI_NMAX + c * 32), acc);
+                    int64_t sv = segv[0];
+#pragma unroll
+                    for (int z = 1; z < TI_NMAX / 32 / 2; ++z)
+                        if (cc == z) sv = segv[z];
+#pragma unroll
+                    for (int j = 0; j < 32; ++j) {
+                        const int64_t seg = __shfl_sync(0xffffffffu, sv, j);
+                        if (seg != INT64_MIN && rok) scores[seg + row] = fmaf(-2.f, acc[j], xn);
+                    }
+                }
+                tc_fence_before();
+                __syncwarp();
+                if (lane == 0) mbar_arrive(accempty + b);
+            }
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (warp == 1) tmem_dealloc(tmem, 512);
+}
+
+typedef CUresult (*EncodeTiledFnI)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                   const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static EncodeTiledFnI encode_fn() {
+    static EncodeTiledFnI fn = nullptr;
+    if (!fn) {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<EncodeTiledFnI>(p);
+    }
+    return fn;
+}
+
+static int tmap(CUtensorMap *m, const void *base, int64_t rows, int K, int box_rows) {
+    EncodeTiledFnI enc = encode_fn();
+    if (!enc) return fail(GN_ERR_CUDA, "cuTensorMapEncodeTiled is unavailable");
+    cuuint64_t dims[2] = {(cuuint64_t)K, (cuuint64_t)rows};
+    cuuint64_t strides[1] = {(cuuint64_t)K * 2};
+    cuuint32_t box[2] = {(cuuint32_t)TI_BK, (cuuint32_t)box_rows};
+    cuuint32_t estr[2] = {1, 1};
+    CUresult r = enc(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void *>(base), dims, strides, box, estr,
+                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return fail(GN_ERR_CUDA, "cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
+    return GN_OK;
+}
+
+int tc_ivf_launch(const TcIvfLaunch &a, cudaStream_t st) {
+    if (a.K % TI_BK) return fail(GN_ERR_INVALID, "tensor-core list scan: K must be a multiple of 64");
+    if (a.x_rows < TI_M || a.q_rows < TI_NMAX) return fail(GN_ERR_INVALID, "tensor-core list scan: buffers too small");
+    CUtensorMap mx, m32, m64, m128, m256;
+    GN_TRY(tmap(&mx, a.X, a.x_rows, a.K, TI_M));
+    GN_TRY(tmap(&m32, a.Q, a.q_rows, a.K, 32));
+    GN_TRY(tmap(&m64, a.Q, a.q_rows, a.K, 64));
+    GN_TRY(tmap(&m128, a.Q, a.q_rows, a.K, 128));
+    GN_TRY(tmap(&m256, a.Q, a.q_rows, a.K, 256));
+    static bool attr = false;
+    if (!attr) {
+        GN_CUDA_TRY(cudaFuncSetAttribute(tc_ivf_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TI_SMEM));
+        attr = true;
+    }
+    tc_ivf_kernel<<<a.grid, TI_THREADS, TI_SMEM, st>>>(mx, m32, m64, m128, m256, a.units, a.n_units, a.K, a.xnorm,
+                                                        a.aslot, a.scores, a.err);
+    GN_CUDA_TRY(cudaGetLastError());
+    return GN_OK;
+}
+
+}  // namespace gn

@@ -1,0 +1,25 @@
+// tc_ivf.cuh — launcher of the tensor-core IVF list scan (see tc_ivf.cu).
+#pragma once
+
+#include "tc_scan.cuh"
+
+namespace gn {
+
+struct TcIvfLaunch {
+    const void *X = nullptr;  // BF16 list rows [x_rows x K] (x_rows >= 128)
+    int64_t x_rows = 0;
+    const void *Q = nullptr;  // BF16 query rows in bucket order [q_rows x K] (q_rows >= 256)
+    int64_t q_rows = 0;
+    int K = 0;                // multiple of 64
+    const TcUnit *units = nullptr;  // a0/na: query rows, r0/r1: list rows, rbase: list start
+    const int64_t *n_units = nullptr;
+    const float *xnorm = nullptr;   // |x|^2 of the list rows
+    const int64_t *aslot = nullptr; // per query row: segment base of its (query, probe) pair
+    float *scores = nullptr;
+    int *err = nullptr;
+    int grid = 0;
+};
+
+int tc_ivf_launch(const TcIvfLaunch &a, cudaStream_t st);
+
+}  // namespace gn
