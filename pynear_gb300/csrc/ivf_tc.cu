@@ -24,6 +24,8 @@
 
 #include "ivf.cuh"
 #include "kmeans.cuh"
+#include "prober.cuh"
+#include "flat_scan.cuh"
 #include "tc_ivf.cuh"
 #include "tc_scan.cuh"
 #include "timing.cuh"
@@ -34,17 +36,18 @@ namespace gn {
 
 constexpr int TC_QCHUNK = 256;  // queries per tensor-core work unit (MMA N <= 256)
 
-__global__ void qb_fill_kernel(const float *__restrict__ Q, int d, int dp, int K, int np,
-                               const int64_t *__restrict__ bucket, const int64_t *__restrict__ boff_end,
-                               const int64_t *__restrict__ qslot, const int64_t *__restrict__ slot_rel,
-                               __nv_bfloat16 *__restrict__ qb, int64_t *__restrict__ aslot, int64_t max_pairs) {
-    const int64_t pos = (int64_t)blockIdx.x;
+// Qb row pos = BF16 row of the query of the pair bucket[pos]; warp per row.
+__global__ void qb_fill_kernel(const uint4 *__restrict__ q16, int K8, int np, const int64_t *__restrict__ bucket,
+                               const int64_t *__restrict__ boff_end, const int64_t *__restrict__ qslot,
+                               const int64_t *__restrict__ slot_rel, uint4 *__restrict__ qb,
+                               int64_t *__restrict__ aslot, int64_t max_pairs) {
+    const int lane = threadIdx.x & 31;
+    const int64_t pos = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     if (pos >= max_pairs || pos >= *boff_end) return;
     const int64_t pair = bucket[pos];
     const int64_t q = pair / np;
-    for (int j = threadIdx.x; j < K; j += blockDim.x)
-        qb[pos * K + j] = __float2bfloat16_rn(j < d ? Q[q * dp + j] : 0.f);
-    if (threadIdx.x == 0) aslot[pos] = qslot[q] + slot_rel[pair];
+    for (int j = lane; j < K8; j += 32) qb[pos * K8 + j] = q16[q * K8 + j];
+    if (lane == 0) aslot[pos] = qslot[q] + slot_rel[pair];
 }
 
 __device__ __forceinline__ int find_list_tc(const int64_t *item_off, int nc, int64_t item) {
@@ -121,35 +124,50 @@ __global__ void ivf_tc_select_kernel(const float *__restrict__ scores, const int
     uint64_t thr = KEY_EMPTY;
     float thr_f = INF;
     if (active) {
-        int64_t blk = 0;  // running index of 128-score blocks over the query's segments
-        for (int p = 0; p < np; ++p) {
-            const int64_t pair = q * np + p;
-            const int32_t l = probes[pair];
-            if (l < 0) continue;
-            const int64_t lb = list_off[l], len = list_off[l + 1] - lb;
-            const float *sc = scores + qseg[q] + seg_rel[pair];
-            const int64_t nblk = (len + 127) / 128;
-            // first block of this segment owned by warp wq
-            int64_t b0 = (wq - blk % W + W) % W;
-            for (int64_t b = b0; b < nblk; b += W) {
-                const int64_t i0 = b * 128;
-                float v[4];
-#pragma unroll
-                for (int u = 0; u < 4; ++u) {
-                    const int64_t i = i0 + u * 32 + lane;
-                    v[u] = (i < len) ? __ldg(sc + i) : INF;
-                }
-                const float m = fminf(fminf(v[0], v[1]), fminf(v[2], v[3]));
-                if (!__any_sync(0xffffffffu, m <= thr_f)) continue;
-#pragma unroll
-                for (int u = 0; u < 4; ++u) {
-                    const int64_t i = i0 + u * 32 + lane;
-                    const uint64_t key = (i < len) ? make_key(f2ord(v[u]), (uint32_t)(lb + i)) : KEY_EMPTY;
-                    L.offer(key, thr, S);
-                    thr_f = (thr == KEY_EMPTY) ? INF : ord2f(key_dist(thr));
+        int64_t blk = 0;  // running index of 256-score blocks over the query's segments
+        for (int p0 = 0; p0 < np; p0 += 32) {
+            // lane p holds probe p0 + p's list start, length and score segment
+            const int p = p0 + lane;
+            int64_t m_lb = 0, m_len = 0;
+            const float *m_sc = nullptr;
+            if (p < np) {
+                const int64_t pair = q * np + p;
+                const int32_t l = probes[pair];
+                if (l >= 0) {
+                    m_lb = list_off[l];
+                    m_len = list_off[l + 1] - m_lb;
+                    m_sc = scores + qseg[q] + seg_rel[pair];
                 }
             }
-            blk += nblk;
+            const int cnt = min(32, np - p0);
+            for (int pp = 0; pp < cnt; ++pp) {
+                const int64_t len = __shfl_sync(0xffffffffu, m_len, pp);
+                if (len == 0) continue;
+                const int64_t lb = __shfl_sync(0xffffffffu, m_lb, pp);
+                const float *sc = reinterpret_cast<const float *>(
+                    __shfl_sync(0xffffffffu, reinterpret_cast<uintptr_t>(m_sc), pp));
+                const int nblk = (int)((len + 255) / 256);
+                const int ilen = (int)len;
+                const int b0 = (int)((wq - blk % W + W) % W);  // first block of this segment owned by warp wq
+                for (int b = b0; b < nblk; b += W) {
+                    const int i0 = b * 256 + lane;
+                    float v[8];
+#pragma unroll
+                    for (int u = 0; u < 8; ++u) v[u] = (i0 + u * 32 < ilen) ? __ldg(sc + i0 + u * 32) : INF;
+                    float m = v[0];
+#pragma unroll
+                    for (int u = 1; u < 8; ++u) m = fminf(m, v[u]);
+                    if (!__any_sync(0xffffffffu, m <= thr_f)) continue;
+#pragma unroll
+                    for (int u = 0; u < 8; ++u) {
+                        const int i = i0 + u * 32;
+                        const uint64_t key = (i < ilen) ? make_key(f2ord(v[u]), (uint32_t)(lb + i)) : KEY_EMPTY;
+                        L.offer(key, thr, S);
+                        thr_f = (thr == KEY_EMPTY) ? INF : ord2f(key_dist(thr));
+                    }
+                }
+                blk += nblk;
+            }
         }
     }
     if (W > 1) {
@@ -191,6 +209,229 @@ __global__ void ivf_tc_select_kernel(const float *__restrict__ scores, const int
     if (lane == 0 && out_cnt) out_cnt[q] = cnt;
 }
 
+// ── tensor-core coarse stage ──────────────────────────────────────────────
+// Units of the centroid scan: every query chunk of 256 against every chunk of
+// 128 centroids; aslot[q] = q * nc so the scores land row-major [nq x nc].
+__global__ void coarse_units_kernel(int64_t nq, int nc, TcUnit *__restrict__ units, int64_t *__restrict__ n_units,
+                                    int64_t *__restrict__ aslot) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t nqc = (nq + 255) / 256, ncc = (nc + 127) / 128;
+    if (t == 0) *n_units = nqc * ncc;
+    if (t < nq) aslot[t] = t * nc;
+    if (t >= nqc * ncc) return;
+    const int64_t qc = t / ncc, cc = t % ncc;
+    TcUnit u;
+    u.a0 = qc * 256;
+    u.na = (int32_t)min((int64_t)256, nq - u.a0);
+    u.r0 = cc * 128;
+    u.r1 = min((int64_t)nc, u.r0 + 128);
+    u.rbase = 0;
+    u.rch = 0;
+    units[t] = u;
+}
+
+constexpr int PROBE_MAX_D = 2048;  // query row staged in shared memory
+
+// Per query (block of 256 threads): the 64 best centroids by BF16 score, their
+// exact squared distances (FP32), sorted nearest first; then either the first
+// np of them (fixed probing) or the learned prober's choice (MLP fused here).
+template <bool MLP>
+__global__ void __launch_bounds__(256) coarse_probe_kernel(const float *__restrict__ scores, int nc, int ncp2,
+                                                           const float *__restrict__ Q, int d, int dp,
+                                                           const float *__restrict__ C, int64_t nq, int np,
+                                                           ProberWeights w, float logit_tau,
+                                                           int32_t *__restrict__ probes,
+                                                           int32_t *__restrict__ nprobed) {
+    constexpr int NC = PROBER_CAND, H = PROBER_HIDDEN;
+    __shared__ int32_t sc[NC];
+    __shared__ float sd[NC], sf[NC], sh1[H], sh2[H], sz[NC];
+    __shared__ int s_cnt0;
+    __shared__ __align__(16) float sqr[PROBE_MAX_D];
+    extern __shared__ uint64_t skeys[];  // next_pow2(nc) keys
+    const int64_t q = blockIdx.x;
+    const int j = threadIdx.x, lane = j & 31, warp = j >> 5;
+    const float *sq = scores + q * nc;
+    for (int t = j; t < d; t += 256) sqr[t] = Q[q * dp + t];
+    // block-wide bitonic sort of the BF16 scores; the first 64 are the candidates
+    for (int c = j; c < ncp2; c += 256) skeys[c] = c < nc ? make_key(f2ord(sq[c]), (uint32_t)c) : KEY_EMPTY;
+    __syncthreads();
+    for (int size = 2; size <= ncp2; size <<= 1)
+        for (int stride = size >> 1; stride > 0; stride >>= 1) {
+            for (int i = j; i < ncp2 / 2; i += 256) {
+                const int lo = 2 * i - (i & (stride - 1)), hi = lo + stride;
+                const bool up = (lo & size) == 0;
+                const uint64_t a = skeys[lo], b = skeys[hi];
+                if ((a > b) == up) { skeys[lo] = b; skeys[hi] = a; }
+            }
+            __syncthreads();
+        }
+    if (j < NC) sc[j] = skeys[j] == KEY_EMPTY ? -1 : (int32_t)key_idx(skeys[j]);
+    __syncthreads();
+    {   // exact squared distances: 4 threads per candidate, float4 strides
+        const int i = j >> 2, part = j & 3;
+        const int c = sc[i];
+        float s0 = 0.f, s1 = 0.f;
+        if (c >= 0) {
+            const float4 *cr = reinterpret_cast<const float4 *>(C + (int64_t)c * dp);
+            const float4 *qr = reinterpret_cast<const float4 *>(sqr);
+            const int n4 = d >> 2;
+#pragma unroll 4
+            for (int t = part; t < n4; t += 8) {
+                const float4 a = __ldg(cr + t), b = qr[t];
+                float e0 = b.x - a.x, e1 = b.y - a.y, e2 = b.z - a.z, e3 = b.w - a.w;
+                s0 = fmaf(e0, e0, s0); s1 = fmaf(e1, e1, s1); s0 = fmaf(e2, e2, s0); s1 = fmaf(e3, e3, s1);
+                if (t + 4 < n4) {
+                    const float4 a2 = __ldg(cr + t + 4), b2 = qr[t + 4];
+                    e0 = b2.x - a2.x; e1 = b2.y - a2.y; e2 = b2.z - a2.z; e3 = b2.w - a2.w;
+                    s0 = fmaf(e0, e0, s0); s1 = fmaf(e1, e1, s1); s0 = fmaf(e2, e2, s0); s1 = fmaf(e3, e3, s1);
+                }
+            }
+            for (int t = (n4 << 2) + part; t < d; t += 4) {  // d % 4 tail
+                const float e = sqr[t] - C[(int64_t)c * dp + t];
+                s0 = fmaf(e, e, s0);
+            }
+        }
+        float s = s0 + s1;
+        s += __shfl_xor_sync(0xffffffffu, s, 1);
+        s += __shfl_xor_sync(0xffffffffu, s, 2);
+        if (part == 0) sd[i] = s;
+    }
+    __syncthreads();
+    if (j < NC) skeys[j] = sc[j] >= 0 ? make_key(__float_as_uint(sd[j]), (uint32_t)sc[j]) : KEY_EMPTY;
+    __syncthreads();
+    for (int size = 2; size <= NC; size <<= 1)
+        for (int stride = size >> 1; stride > 0; stride >>= 1) {
+            if (j < NC / 2) {
+                const int lo = 2 * j - (j & (stride - 1)), hi = lo + stride;
+                const bool up = (lo & size) == 0;
+                const uint64_t a = skeys[lo], b = skeys[hi];
+                if ((a > b) == up) { skeys[lo] = b; skeys[hi] = a; }
+            }
+            __syncthreads();
+        }
+    if (j < NC) {
+        const uint64_t k = skeys[j];
+        const bool e = k == KEY_EMPTY;
+        const float d1 = __uint_as_float(key_dist(skeys[0]));
+        sc[j] = e ? -1 : (int32_t)key_idx(k);
+        sf[j] = e ? 0.f : fmaxf(0.f, 1.f - (__uint_as_float(key_dist(k)) - d1) / fmaxf(d1, 1e-12f));
+    }
+    __syncthreads();
+    if (!MLP) {
+        if (j < np) probes[q * np + j] = sc[j];
+        return;
+    }
+    const __nv_bfloat16 *W1 = reinterpret_cast<const __nv_bfloat16 *>(w.W1);
+    const __nv_bfloat16 *W2 = reinterpret_cast<const __nv_bfloat16 *>(w.W2);
+    const __nv_bfloat16 *W3 = reinterpret_cast<const __nv_bfloat16 *>(w.W3);
+    float a = w.b1[j];
+    for (int i = 0; i < NC; ++i)
+        if (sc[i] >= 0) a = fmaf(sf[i], __bfloat162float(W1[(size_t)sc[i] * H + j]), a);
+    sh1[j] = fmaxf(a, 0.f);
+    __syncthreads();
+    for (int o = warp * 32; o < warp * 32 + 32; ++o) {
+        float s = 0.f;
+#pragma unroll
+        for (int k = lane; k < H; k += 32) s = fmaf(__bfloat162float(W2[(size_t)o * H + k]), sh1[k], s);
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
+        if (lane == 0) sh2[o] = fmaxf(s + w.b2[o], 0.f);
+    }
+    __syncthreads();
+    for (int i = warp; i < NC; i += 8) {
+        const int c = sc[i];
+        float s = 0.f;
+        if (c >= 0) {
+#pragma unroll
+            for (int k = lane; k < H; k += 32) s = fmaf(__bfloat162float(W3[(size_t)c * H + k]), sh2[k], s);
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
+        }
+        if (lane == 0) sz[i] = c >= 0 ? s + w.b3[c] : -INFINITY;
+    }
+    __syncthreads();
+    bool keep = false;
+    unsigned m = 0;
+    const int i = warp * 32 + lane;
+    if (warp < NC / 32) {
+        keep = sc[i] >= 0 && (i == 0 || sz[i] >= logit_tau);
+        m = __ballot_sync(0xffffffffu, keep);
+        if (warp == 0 && lane == 0) s_cnt0 = __popc(m);
+    }
+    __syncthreads();
+    if (warp < NC / 32) {
+        const int pos = (warp == 0 ? 0 : s_cnt0) + __popc(m & ((1u << lane) - 1u));
+        if (keep) probes[q * NC + pos] = sc[i];
+        if (warp == 1) {
+            const int total = s_cnt0 + __popc(m);
+            for (int t = total + lane; t < NC; t += 32) probes[q * NC + t] = -1;
+            if (lane == 0 && nprobed) nprobed[q] = total;
+        }
+    }
+}
+
+// Probes of the tensor-core engine: BF16 centroid scores on the tensor cores,
+// exact re-rank of the 64 best, then fixed n_probe or the learned prober.
+static int ivfl2_probes_tc(gn_index *ix, const float *dQ, int64_t nq, int *np_out, cudaStream_t st) {
+    IvfL2State &S = *ix->ivfl2;
+    IvfScratch &T = S.s;
+    if (S.nc < PROBER_CAND || S.d > PROBE_MAX_D || S.nc > 8192) {  // outside the 64-candidate stage's limits
+        if (S.prober) return fail(GN_ERR_INVALID, "learned probing needs at least 64 lists");
+        int np = std::min<int32_t>(S.nprobe, S.nc);
+        *np_out = np;
+        return ivfl2_coarse(ix, dQ, nq, np, st);
+    }
+    const bool mlp = S.prober != nullptr;
+    const int np = mlp ? PROBER_CAND : std::min<int32_t>(std::min<int32_t>(S.nprobe, S.nc), PROBER_CAND);
+    if (!mlp && S.nprobe > PROBER_CAND) {  // wider fixed probing: the FP32 coarse stage
+        *np_out = std::min<int32_t>(S.nprobe, S.nc);
+        return ivfl2_coarse(ix, dQ, nq, *np_out, st);
+    }
+    *np_out = np;
+    const int64_t units = ceil_div(nq, 256) * ceil_div(S.nc, 128);
+    GN_TRY(S.cunits.ensure((size_t)units * sizeof(TcUnit)));
+    GN_TRY(S.cnunits.ensure(8));
+    GN_TRY(S.caslot.ensure((size_t)nq * 8));
+    GN_TRY(S.cscores.ensure((size_t)nq * S.nc * 4));
+    GN_TRY(T.probes.ensure((size_t)nq * np * 4));
+    coarse_units_kernel<<<(unsigned)ceil_div(std::max<int64_t>(units, nq), 256), 256, 0, st>>>(
+        nq, S.nc, S.cunits.as<TcUnit>(), S.cnunits.as<int64_t>(), S.caslot.as<int64_t>());
+    TcIvfLaunch a;
+    a.X = S.c16.p;
+    a.x_rows = std::max<int64_t>(S.nc, 128);
+    a.Q = S.q16.p;
+    a.q_rows = std::max<int64_t>(nq, 256);
+    a.K = S.K;
+    a.units = S.cunits.as<TcUnit>();
+    a.n_units = S.cnunits.as<int64_t>();
+    a.xnorm = S.cnorm.as<float>();
+    a.aslot = S.caslot.as<int64_t>();
+    a.scores = S.cscores.as<float>();
+    a.err = S.err.as<int>();
+    a.grid = (int)std::min<int64_t>(dev_info().num_sms, units);
+    GN_TRY(tc_ivf_launch(a, st));
+    const int ncp2 = (int)next_pow2(S.nc);
+    const size_t ksm = (size_t)ncp2 * 8;
+    if (ksm > 48 * 1024) {
+        GN_CUDA_TRY(cudaFuncSetAttribute(coarse_probe_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ksm));
+        GN_CUDA_TRY(cudaFuncSetAttribute(coarse_probe_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ksm));
+    }
+    ProberWeights w;
+    if (mlp) {
+        GN_TRY(prober_weights(S.prober, &w));
+        GN_TRY(T.nprobed.ensure((size_t)nq * 4));
+        coarse_probe_kernel<true><<<(unsigned)nq, 256, ksm, st>>>(S.cscores.as<float>(), S.nc, ncp2, dQ, S.d, S.dp,
+                                                               S.cent.as<float>(), nq, np, w, S.prober_tau,
+                                                               T.probes.as<int32_t>(), T.nprobed.as<int32_t>());
+    } else {
+        coarse_probe_kernel<false><<<(unsigned)nq, 256, ksm, st>>>(S.cscores.as<float>(), S.nc, ncp2, dQ, S.d, S.dp,
+                                                                S.cent.as<float>(), nq, np, w, 0.f,
+                                                                T.probes.as<int32_t>(), nullptr);
+    }
+    GN_CUDA_TRY(cudaGetLastError());
+    return GN_OK;
+}
+
 int ivfl2_prepare_tc(gn_index *ix, cudaStream_t st) {
     IvfL2State &S = *ix->ivfl2;
     S.K = (int)round_up(S.d, 64);
@@ -198,6 +439,10 @@ int ivfl2_prepare_tc(gn_index *ix, cudaStream_t st) {
     GN_TRY(S.x16.ensure((size_t)rows * S.K * 2));
     GN_CUDA_TRY(cudaMemsetAsync(S.x16.p, 0, (size_t)rows * S.K * 2, st));
     to_bf16_rows(S.vecs.as<float>(), S.n, S.d, S.dp, S.x16.p, S.K, st);
+    const int64_t crows = std::max<int64_t>(S.nc, 128);  // at least one 128-row TMA box
+    GN_TRY(S.c16.ensure((size_t)crows * S.K * 2));
+    GN_CUDA_TRY(cudaMemsetAsync(S.c16.p, 0, (size_t)crows * S.K * 2, st));
+    to_bf16_rows(S.cent.as<float>(), S.nc, S.d, S.dp, S.c16.p, S.K, st);
     GN_TRY(S.err.ensure(4));
     GN_CUDA_TRY(cudaMemsetAsync(S.err.p, 0, 4, st));
     GN_CUDA_TRY(cudaGetLastError());
@@ -210,8 +455,10 @@ int ivfl2_search_tc(gn_index *ix, const float *dQ, int64_t nq, int k, int64_t *d
     IvfScratch &T = S.s;
     if (k > 32 || k > S.shortlist) return fail(GN_ERR_UNSUPPORTED, "tensor-core IVF supports k <= min(32, shortlist)");
     if (S.K == 0) GN_TRY(ivfl2_prepare_tc(ix, st));
+    GN_TRY(S.q16.ensure((size_t)std::max<int64_t>(nq, 256) * S.K * 2));
+    to_bf16_rows(dQ, nq, S.d, S.dp, S.q16.p, S.K, st);
     int np = 1;
-    GN_TRY(ivfl2_probes(ix, dQ, nq, &np, st));
+    GN_TRY(ivfl2_probes_tc(ix, dQ, nq, &np, st));
     // work items of rc rows (short items for small batches so that their few
     // lists still spread over all SMs); every pair owns a score segment
     const int rc = nq >= 512 ? S.rc_tc : (nq >= 64 ? 1024 : 256);
@@ -220,10 +467,9 @@ int ivfl2_search_tc(gn_index *ix, const float *dQ, int64_t nq, int k, int64_t *d
     const int64_t qb_rows = std::max<int64_t>(npairs, 256);  // >= one 256-row TMA box
     GN_TRY(S.qb.ensure((size_t)qb_rows * S.K * 2));
     GN_TRY(S.aslot.ensure((size_t)npairs * 8));
-    qb_fill_kernel<<<(unsigned)npairs, 128, 0, st>>>(dQ, S.d, S.dp, S.K, np, T.bucket.as<int64_t>(),
-                                                     T.boff.as<int64_t>() + S.nc, T.qslot.as<int64_t>(),
-                                                     T.slot_rel.as<int64_t>(), S.qb.as<__nv_bfloat16>(),
-                                                     S.aslot.as<int64_t>(), npairs);
+    qb_fill_kernel<<<(unsigned)ceil_div(npairs, 8), 256, 0, st>>>(
+        S.q16.as<uint4>(), S.K / 8, np, T.bucket.as<int64_t>(), T.boff.as<int64_t>() + S.nc, T.qslot.as<int64_t>(),
+        T.slot_rel.as<int64_t>(), S.qb.as<uint4>(), S.aslot.as<int64_t>(), npairs);
     const int64_t maxlen = S.top_rows.size() > 1 ? S.top_rows[1] : 0;
     const int64_t max_units = (ceil_div(npairs, TC_QCHUNK) + S.nc) * (ceil_div(maxlen, rc) + 1);
     GN_TRY(S.units.ensure((size_t)max_units * sizeof(TcUnit)));
@@ -252,7 +498,7 @@ int ivfl2_search_tc(gn_index *ix, const float *dQ, int64_t nq, int k, int64_t *d
     timing_end(st);
     // warps per query: enough warps in flight for small batches
     int W = 1;
-    while (W < 16 && nq * W * 2 <= (int64_t)dev_info().num_sms * 32) W *= 2;
+    while (W < 16 && nq * W <= (int64_t)dev_info().num_sms * 64) W *= 2;
     const int qpb = std::max(1, 8 / W);
     const int threads = 32 * W * qpb;
     const unsigned blocks = (unsigned)ceil_div(nq, qpb);

@@ -404,6 +404,20 @@ int prober_apply(gn_index *pr, gn_index *ivf, const float *dQ, int64_t nq, float
     return GN_OK;
 }
 
+int prober_weights(gn_index *pr, ProberWeights *w) {
+    if (!pr || pr->kind != K_PROBER) return fail(GN_ERR_INVALID, "not a prober");
+    ProberState &P = *pst(pr);
+    const __nv_bfloat16 *wb = P.wbf.as<__nv_bfloat16>();
+    const float *pf = P.params.as<float>();
+    w->W1 = wb + P.oW1;
+    w->W2 = wb + P.oW2;
+    w->W3 = wb + P.oW3;
+    w->b1 = pf + P.ob1;
+    w->b2 = pf + P.ob2;
+    w->b3 = pf + P.ob3;
+    return GN_OK;
+}
+
 }  // namespace gn
 
 using namespace gn;
