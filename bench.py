@@ -5,11 +5,14 @@
 Headline workload (batched IVF-flat L2): database 1,000,000 x 512 float32 drawn
 from a Gaussian mixture of 2,048 centres N(0, I) with Zipf(1.1) component
 sizes and noise sigma = 0.3; nlist = 1,024 lists built by the library's GPU
-k-means; k = 10.  Query batches have log-uniform random sizes 1..4,096.  For
-each engine the smallest nprobe whose Recall@10 (against exact flat search on
-held-out calibration queries) reaches 0.95 is used:
-  plain  FP32 CUDA-core list scan (the reference's |q|^2+|x|^2-2q.x form);
-  tuned  BF16 tcgen05 shortlist of 40 + exact FP32 re-rank.
+k-means; k = 10.  Query batches have log-uniform random sizes 1..4,096.  Each
+engine runs at its cheapest setting whose Recall@10 (against exact flat search
+on 2,000 held-out calibration queries) reaches 0.95:
+  plain  fixed nprobe, FP32 CUDA-core list scan (the reference's
+         |q|^2+|x|^2-2q.x form): the smallest such nprobe;
+  tuned  learned probing (MLP trained on the GPU on 200,000 mixture queries
+         labelled by exact GPU search) + BF16 tcgen05 shortlist of 40 + exact
+         FP32 re-rank: the largest such probability threshold.
 A step is one pass over a fixed sequence of batches (16,384 queries).  `value`
 is the tuned engine's throughput with queries resident in HBM; `e2e` repeats it
 through the C ABI with pinned host buffers (copies inside the timed region).
@@ -44,7 +47,9 @@ METRIC = "QPS @ Recall@10>=0.95 (1M x 512 f32, k=10): tuned vs plain GPU scan; H
 POPC_PER_CLK_PER_SM = 16  # 32-bit population count throughput per SM per clock
 IVF_N, IVF_D, IVF_CENTRES, IVF_NLIST, K = 1_000_000, 512, 2048, 1024, 10
 N_CAL, N_EVAL, STEP_QUERIES = 2000, 2000, 16384
+N_TRAIN = 200_000
 NPROBES = [1, 2, 4, 6, 8, 12, 16, 20, 24, 28, 32, 40, 48, 64]
+PROB_THRESHOLDS = [0.5, 0.4, 0.3, 0.25, 0.22, 0.2, 0.19, 0.18, 0.17, 0.16, 0.15, 0.12, 0.1, 0.05, 0.02]
 
 
 # ── environment helpers ───────────────────────────────────────────────────
@@ -230,9 +235,10 @@ def bench_ivf(args, dist, peaks, peak_src):
                 kms += t.value
         return kms
 
-    def timed(engine, nprobe, steps, warmup):
+    def timed(engine, nprobe, steps, warmup, thr=None):
         ix.set_engine(engine)
         ix.n_probe = nprobe
+        ix.set_prober(prober if thr is not None else None, thr if thr is not None else 0.5)
         for _ in range(warmup):
             run_step()
         torch.cuda.synchronize()
@@ -254,19 +260,48 @@ def bench_ivf(args, dist, peaks, peak_src):
         lib.gn_timing_enable(0)
         idx, _, _ = ix.search_knn_arrays(ev, K)
         rec = recall_at(idx, gt_ev)
+        lists = float(ix.last_lists_probed(len(ev)).mean()) if thr is not None else float(nprobe)
         return {"qps": STEP_QUERIES * steps * dist.ws / tot, "ms_per_step": statistics.mean(ms), "steps_ms": ms,
-                "kernel_ms_per_step": kern, "recall_eval": rec}
+                "kernel_ms_per_step": kern, "recall_eval": rec, "mean_lists_probed": lists}
 
     plain_p, plain_cal = calibrate("fp32")
-    tuned_p, tuned_cal = calibrate("tc")
+    tcfix_p, tcfix_cal = calibrate("tc")
+    # learned prober: exact labels for 200k training queries, GPU training
+    from pynear_gb300 import workloads as W
+    t0 = time.perf_counter()
+    # training queries come from the database's own mixture (same centres)
+    train_q = W.gaussian_mixture_queries(n=IVF_N, d=IVF_D, n_centres=IVF_CENTRES, sigma=0.3, zipf_s=1.1,
+                                         nq=N_TRAIN, seed=dist.rank, query_seed=99991 + dist.rank)
+    tcx = gn.FlatL2TCIndex(shortlist=40)
+    tcx.set(db)
+    gt_train = np.concatenate([tcx.search_knn_arrays(train_q[i:i + 20000], K)[0] for i in range(0, N_TRAIN, 20000)])
+    del tcx
+    label_s = time.perf_counter() - t0
+    ix.set_engine("tc")
+    prober = gn.LearnedProber(ix, seed=1)
+    t0 = time.perf_counter()
+    losses = prober.train(train_q, gt_train, epochs=4, batch=1024, lr=2e-3)
+    train_s = time.perf_counter() - t0
+    del train_q, gt_train
+    learned_cal, thr_sel = [], PROB_THRESHOLDS[-1]
+    for thr in PROB_THRESHOLDS:
+        ix.set_prober(prober, thr)
+        idx, _, _ = ix.search_knn_arrays(cal, K)
+        r = recall_at(idx, gt_cal)
+        learned_cal.append((thr, r, float(ix.last_lists_probed(len(cal)).mean())))
+        if r >= 0.95:
+            thr_sel = thr
+            break
+    ix.set_prober(None)
     sampler = ClockSampler(dev.index).start()
     plain = timed("fp32", plain_p, max(2, args.steps // 2), args.warmup)
-    tuned = timed("tc", tuned_p, args.steps, args.warmup)
+    tcfix = timed("tc", tcfix_p, max(2, args.steps // 2), args.warmup)
+    tuned = timed("tc", tcfix_p, args.steps, args.warmup, thr=thr_sel)
     clocks = sampler.stop()
 
     # work accounting for the roofline: one full-size batch of the tuned engine
     ix.set_engine("tc")
-    ix.n_probe = tuned_p
+    ix.set_prober(prober, thr_sel)
     nb = min(4096, len(stepq))
     _lib.check(lib.gn_ivfl2_search_knn_device(ix._h.h, vp(d_q), nb, K, vp(d_idx), vp(d_dist), vp(d_cnt),
                                               ctypes.c_void_p(stream.cuda_stream)))
@@ -282,13 +317,14 @@ def bench_ivf(args, dist, peaks, peak_src):
     pairs, scored, rows, units = (int(x) for x in w)
     kpad = ((IVF_D + 63) // 64) * 64
     bytes_alg = rows * kpad * 2 + scored * 4          # BF16 list rows read once + FP32 scores written
+    name_v = name.value.decode()
     flops_alg = 2.0 * IVF_D * scored                 # useful MACs x 2
     kms = t.value
     hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
     tc_peak = float(peaks.get("bf16_tflops_sustained", peaks.get("bf16_tflops", 1700.0)))
     achieved_gbs = bytes_alg / (kms / 1e3) / 1e9
-    roofline = {"bound": "hbm", "kernel": name.value.decode(), "achieved": achieved_gbs, "peak": hbm_peak,
-                "unit": "GB/s", "frac": achieved_gbs / hbm_peak, "traffic": profile_traffic("tc_topk_kernel<store>"),
+    roofline = {"bound": "hbm", "kernel": name_v, "achieved": achieved_gbs, "peak": hbm_peak,
+                "unit": "GB/s", "frac": achieved_gbs / hbm_peak, "traffic": profile_traffic(name_v),
                 "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)",
                 "kernel_ms": kms, "batch_queries": nb,
                 "algorithmic_per_launch": {"bytes": int(bytes_alg), "flops": flops_alg, "pairs": pairs,
@@ -307,6 +343,8 @@ def bench_ivf(args, dist, peaks, peak_src):
             qp = ctypes.c_void_p(h_q.data_ptr() + int(o) * IVF_D * 4)
             _lib.check(lib.gn_ivfl2_search_knn(ix._h.h, qp, int(nb_), K, vp(h_idx), vp(h_dist), vp(h_cnt)))
 
+    ix.set_engine("tc")
+    ix.set_prober(prober, thr_sel)
     e2e_step()
     dist.barrier()
     t0 = time.perf_counter()
@@ -315,10 +353,14 @@ def bench_ivf(args, dist, peaks, peak_src):
     e2e_s = dist.max(time.perf_counter() - t0)
     e2e = {"value": STEP_QUERIES * args.steps * dist.ws / e2e_s, "unit": "queries/s",
            "h2d_bytes_per_step": int(stepq.nbytes), "d2h_bytes_per_step": int(STEP_QUERIES * K * (8 + 4) + STEP_QUERIES * 8)}
-    launches_per_batch = 11  # norms, coarse, 5 planning, Qb, units, tensor-core scan, select
+    launches_per_batch = 13  # BF16 queries, coarse units, coarse scan, coarse+MLP, 5 planning, Qb, units, scan, select
     cent, offs_l, ids = ix.export()
-    return {"tuned": tuned, "plain": plain, "tuned_nprobe": tuned_p, "plain_nprobe": plain_p,
-            "calibration": {"fp32": plain_cal, "tc": tuned_cal}, "roofline": roofline, "e2e": e2e,
+    return {"tuned": tuned, "plain": plain, "tc_fixed": tcfix, "tuned_nprobe": tcfix_p, "plain_nprobe": plain_p,
+            "tuned_threshold": thr_sel,
+            "prober": {"train_queries": N_TRAIN, "epochs": 4, "losses": [float(x) for x in losses],
+                       "label_s": label_s, "train_s": train_s},
+            "calibration": {"fp32": plain_cal, "tc_fixed": tcfix_cal, "learned": learned_cal},
+            "roofline": roofline, "e2e": e2e,
             "clocks": clocks, "build_s": build_s, "gen_s": gen_s, "n_batches": len(batches),
             "gpu_launches": launches_per_batch * len(batches) * args.steps,
             "index": (db, cent, offs_l, ids), "eval": ev, "gt_eval": gt_ev}
@@ -509,13 +551,16 @@ def main():
                        "nlist": IVF_NLIST, "k": K, "queries_per_step": STEP_QUERIES,
                        "batches_per_step": ivf["n_batches"], "batch_sizes": "log-uniform 1..4096",
                        "tuned": {"engine": "tc (BF16 tcgen05 shortlist 40 + exact FP32 re-rank)",
-                                 "nprobe": ivf["tuned_nprobe"]},
+                                 "probing": "learned MLP", "prob_threshold": ivf["tuned_threshold"],
+                                 "mean_lists_probed": t["mean_lists_probed"]},
                        "plain": {"engine": "fp32 CUDA-core scan", "nprobe": ivf["plain_nprobe"]},
                        "l2": "index data (3 GB) exceeds L2; no flush", "parallelism": f"replicas x{ws}"},
             "recall_at_10": {"tuned": t["recall_eval"], "plain": p["recall_eval"],
                              "calibration": ivf["calibration"]},
             "plain": {"value": p["qps"], "ms_per_step": p["ms_per_step"], "nprobe": ivf["plain_nprobe"]},
-            "tuned_over_plain": t["qps"] / p["qps"],
+            "tc_fixed_nprobe": {"value": ivf["tc_fixed"]["qps"], "nprobe": ivf["tuned_nprobe"],
+                                "recall_at_10": ivf["tc_fixed"]["recall_eval"]},
+            "tuned_over_plain": t["qps"] / p["qps"], "prober": ivf["prober"],
             "roofline": ivf["roofline"], "cpu_baseline": cb, "e2e": ivf["e2e"],
             "gpu_launches": ivf["gpu_launches"], "clocks": ivf["clocks"],
             "build_s": ivf["build_s"], "hamming": ham,

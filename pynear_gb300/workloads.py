@@ -75,3 +75,13 @@ def log_uniform_batches(total, lo=1, hi=4096, seed=0):
         out.append(b)
         s += b
     return out
+
+
+def gaussian_mixture_queries(n=1_000_000, d=512, n_centres=2048, sigma=0.3, zipf_s=1.1, nq=10_000, seed=0,
+                             query_seed=1):
+    """Queries from the same mixture as gaussian_mixture(n, ..., seed) without
+    building the database (same centres, same component weights)."""
+    rng = np.random.default_rng(seed)
+    centres = rng.standard_normal((n_centres, d), dtype=np.float32)
+    sizes = zipf_sizes(n, n_centres, zipf_s) if zipf_s else np.full(n_centres, max(1, n // n_centres), np.int64)
+    return mixture_queries(centres, sizes, nq, sigma, query_seed)
