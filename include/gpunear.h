@@ -74,6 +74,21 @@ int gn_flat_search_1nn(gn_index *ix, const void *queries, int64_t nq, int64_t *o
 int gn_flat_search_knn_device(gn_index *ix, const void *d_queries, int64_t nq, int64_t k, int64_t *d_idx,
                               void *d_dist, void *stream);
 int gn_index_size(gn_index *ix, int64_t *n, int64_t *dim);
+/* Exact Hamming k-NN that allocates no device memory.  No counterpart in the
+ * reference: it is for callers that cannot call cudaMalloc at search time (a
+ * process whose device memory is already owned by another allocator, or a
+ * latency-critical loop that cannot take cudaMalloc's synchronisation).  All
+ * arguments are device buffers: d_db n rows of nbytes (a multiple of 16)
+ * packed bytes, d_queries nq rows of the same width, d_idx / d_dist nq*k int64
+ * results (nearest first, ties to the lower row).  The only other memory used
+ * is a fixed 16 MB array per device inside the library, so nq * k must be at
+ * most 2 Mi (larger requests fail with GN_ERR_INVALID); 1 <= k <= 256.  The
+ * first call on a device looks up that array's address (cudaGetSymbolAddress),
+ * so make it before any stream capture.  Every call uses the same array: calls
+ * that overlap on the GPU (other streams, other threads) race and must be
+ * serialised by the caller.  Returns without synchronising `stream`. */
+int gn_hamming_knn_noalloc(const uint8_t *d_db, int64_t n, int64_t nbytes, const uint8_t *d_queries, int64_t nq,
+                           int64_t k, int64_t *d_idx, int64_t *d_dist, void *stream);
 int gn_index_destroy(gn_index *ix);
 
 /* ── exact L2 via a tensor-core shortlist ─────────────────────────────────
