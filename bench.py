@@ -235,10 +235,12 @@ def bench_ivf(args, dist, peaks, peak_src):
                 kms += t.value
         return kms
 
-    def timed(engine, nprobe, steps, warmup, thr=None):
+    def timed(engine, nprobe, steps, warmup, thr=None, graphs=True):
         ix.set_engine(engine)
         ix.n_probe = nprobe
         ix.set_prober(prober if thr is not None else None, thr if thr is not None else 0.5)
+        # one captured CUDA graph per batch size, captured during the warm-up
+        ix.enable_graphs(nmax if graphs else 0, K)
         for _ in range(warmup):
             run_step()
         torch.cuda.synchronize()
@@ -261,8 +263,10 @@ def bench_ivf(args, dist, peaks, peak_src):
         idx, _, _ = ix.search_knn_arrays(ev, K)
         rec = recall_at(idx, gt_ev)
         lists = float(ix.last_lists_probed(len(ev)).mean()) if thr is not None else float(nprobe)
+        ginfo = ix.graph_info()
         return {"qps": STEP_QUERIES * steps * dist.ws / tot, "ms_per_step": statistics.mean(ms), "steps_ms": ms,
-                "kernel_ms_per_step": kern, "recall_eval": rec, "mean_lists_probed": lists}
+                "kernel_ms_per_step": kern, "recall_eval": rec, "mean_lists_probed": lists, "cuda_graphs": graphs,
+                "graphs_cached": ginfo["graphs"], "graph_capture_failures": ginfo["capture_failures"]}
 
     plain_p, plain_cal = calibrate("fp32")
     tcfix_p, tcfix_cal = calibrate("tc")
@@ -297,6 +301,7 @@ def bench_ivf(args, dist, peaks, peak_src):
     plain = timed("fp32", plain_p, max(2, args.steps // 2), args.warmup)
     tcfix = timed("tc", tcfix_p, max(2, args.steps // 2), args.warmup)
     tuned = timed("tc", tcfix_p, args.steps, args.warmup, thr=thr_sel)
+    tuned_ng = timed("tc", tcfix_p, max(2, args.steps // 2), args.warmup, thr=thr_sel, graphs=False)
     clocks = sampler.stop()
 
     # work accounting for the roofline: one full-size batch of the tuned engine
@@ -345,6 +350,7 @@ def bench_ivf(args, dist, peaks, peak_src):
 
     ix.set_engine("tc")
     ix.set_prober(prober, thr_sel)
+    ix.enable_graphs(nmax, K)
     e2e_step()
     dist.barrier()
     t0 = time.perf_counter()
@@ -355,7 +361,9 @@ def bench_ivf(args, dist, peaks, peak_src):
            "h2d_bytes_per_step": int(stepq.nbytes), "d2h_bytes_per_step": int(STEP_QUERIES * K * (8 + 4) + STEP_QUERIES * 8)}
     launches_per_batch = 13  # BF16 queries, coarse units, coarse scan, coarse+MLP, 5 planning, Qb, units, scan, select
     cent, offs_l, ids = ix.export()
-    return {"tuned": tuned, "plain": plain, "tc_fixed": tcfix, "tuned_nprobe": tcfix_p, "plain_nprobe": plain_p,
+    ix.enable_graphs(0, 0)
+    return {"tuned": tuned, "plain": plain, "tc_fixed": tcfix, "tuned_no_graphs": tuned_ng,
+            "tuned_nprobe": tcfix_p, "plain_nprobe": plain_p,
             "tuned_threshold": thr_sel,
             "prober": {"train_queries": N_TRAIN, "epochs": 4, "losses": [float(x) for x in losses],
                        "label_s": label_s, "train_s": train_s},
@@ -560,6 +568,9 @@ def main():
             "plain": {"value": p["qps"], "ms_per_step": p["ms_per_step"], "nprobe": ivf["plain_nprobe"]},
             "tc_fixed_nprobe": {"value": ivf["tc_fixed"]["qps"], "nprobe": ivf["tuned_nprobe"],
                                 "recall_at_10": ivf["tc_fixed"]["recall_eval"]},
+            "cuda_graphs": {"per_batch": "one captured graph per batch size, replayed",
+                            "graphs_cached": t["graphs_cached"], "capture_failures": t["graph_capture_failures"],
+                            "tuned_without_graphs": ivf["tuned_no_graphs"]["qps"]},
             "tuned_over_plain": t["qps"] / p["qps"], "prober": ivf["prober"],
             "roofline": ivf["roofline"], "cpu_baseline": cb, "e2e": ivf["e2e"],
             "gpu_launches": ivf["gpu_launches"], "clocks": ivf["clocks"],

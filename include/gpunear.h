@@ -135,9 +135,20 @@ int gn_ivfl2_set_assigned(gn_index *ix, const float *data, int64_t n, int64_t d,
                           int32_t n_centroids, const int32_t *labels);
 int gn_ivfl2_search_knn(gn_index *ix, const float *queries, int64_t nq, int64_t k, int64_t *out_idx,
                         float *out_dist, int64_t *out_cnt);
+/* device variant: queries [nq x d] row-major on the device; results written
+ * to device buffers in stream order (no synchronisation) */
 int gn_ivfl2_search_knn_device(gn_index *ix, const float *d_queries, int64_t nq, int64_t k, int64_t *d_idx,
                                float *d_dist, int64_t *d_cnt, void *stream);
 int gn_ivfl2_set_n_probe(gn_index *ix, int32_t n_probe);
+/* CUDA-graph replay (no reference counterpart; same results): searches of
+ * 1..max_batch queries with this k run as one captured graph per batch size,
+ * replayed on fixed staging buffers; a configuration change or a scratch
+ * reallocation drops the cached graphs.  max_batch 0 disables.  The call runs
+ * one search of max_batch queries to size the scratch. */
+int gn_ivfl2_enable_graphs(gn_index *ix, int64_t max_batch, int32_t k);
+/* out[0] max_batch (0: disabled), out[1] cached graphs, out[2] replays,
+ * out[3] captures that failed (those batches ran uncaptured) */
+int gn_ivfl2_graph_info(gn_index *ix, int64_t *out);
 /* Search engine (no reference counterpart; same result contract):
  *   mode 0  FP32 CUDA-core scan, distances |q|^2 + |x|^2 - 2 q.x clamped at 0,
  *           the formula of forest.py:189-194;

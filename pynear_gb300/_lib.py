@@ -60,6 +60,8 @@ SIGNATURES = {
     "gn_ivfl2_set_assigned": [P, P, I64, I64, P, I32, P],
     "gn_ivfl2_search_knn": [P, P, I64, I64, P, P, P],
     "gn_ivfl2_search_knn_device": [P, P, I64, I64, P, P, P, P],
+    "gn_ivfl2_enable_graphs": [P, I64, I32],
+    "gn_ivfl2_graph_info": [P, P],
     "gn_ivfl2_set_n_probe": [P, I32],
     "gn_ivfl2_set_mode": [P, I32, I32],
     "gn_ivfl2_error": [P, P],

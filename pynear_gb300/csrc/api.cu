@@ -1,5 +1,6 @@
 // api.cu — C ABI: status plumbing, device buffers and the exact flat index.
 #include <algorithm>
+#include <atomic>
 #include <cstring>
 #include <string>
 
@@ -29,8 +30,12 @@ const DevInfo &dev_info() {
     return di;
 }
 
+static std::atomic<uint64_t> g_dbuf_gen{1};
+uint64_t dbuf_generation() { return g_dbuf_gen.load(std::memory_order_relaxed); }
+
 int DBuf::ensure(size_t bytes) {
     if (bytes <= cap && p) return GN_OK;
+    g_dbuf_gen.fetch_add(1, std::memory_order_relaxed);  // device pointers held elsewhere may go stale
     release();
     size_t want = std::max<size_t>(bytes, 256);
     cudaError_t e = cudaMalloc(&p, want);

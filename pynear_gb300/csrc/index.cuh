@@ -63,6 +63,9 @@ struct gn_index {
 namespace gn {
 
 int make_stream(gn_index *ix);
+// Counter bumped whenever any DBuf (re)allocates: captured CUDA graphs that
+// hold device pointers compare it to know whether they are still valid.
+uint64_t dbuf_generation();
 void ivf_free(gn_index *ix);
 // Copy n rows of `dim` elements of `elem` bytes from host into a device buffer
 // with row stride stride4*16 bytes, zero padding the tail of each row.

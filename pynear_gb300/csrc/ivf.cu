@@ -564,6 +564,7 @@ static int ivfl2_build_from_labels(gn_index *ix, const float *dX, int64_t n, int
     csr_from_labels(labels, ncent, order, perm, S.h_off);
     S.nc = (int32_t)order.size();
     S.K = 0;  // BF16 copy for the tensor-core engine is rebuilt on first use
+    S.cfg++;
     S.n = n;
     S.d = d;
     S.dp = dp;
@@ -659,8 +660,8 @@ int ivfl2_probes(gn_index *ix, const float *dQ, int64_t nq, int *np_out, cudaStr
 static int ivfl2_scan_fp32(gn_index *ix, const float *dQ, int64_t nq, int np, int k, int64_t *d_idx, float *d_dist,
                            int64_t *d_cnt, cudaStream_t st);
 
-static int ivfl2_search_dev(gn_index *ix, const float *dQ, int64_t nq, int k, int64_t *d_idx, float *d_dist,
-                            int64_t *d_cnt, cudaStream_t st) {
+int ivfl2_search_core(gn_index *ix, const float *dQ, int64_t nq, int k, int64_t *d_idx, float *d_dist,
+                      int64_t *d_cnt, cudaStream_t st) {
     IvfL2State &S = *ix->ivfl2;
     IvfScratch &T = S.s;
     const int np = std::min<int32_t>(S.nprobe, S.nc);
@@ -763,6 +764,7 @@ static int ivfbin_search_dev(gn_index *ix, const uint8_t *dQ, int64_t nq, int k,
 }
 
 void ivf_free(gn_index *ix) {
+    if (ix->ivfl2) delete ix->ivfl2->graphs;
     delete ix->ivfl2;
     delete ix->ivfbin;
     ix->ivfl2 = nullptr;
@@ -874,7 +876,16 @@ int gn_ivfl2_search_knn_device(gn_index *ix, const float *d_queries, int64_t nq,
     if (ix->ivfl2->nc == 0) return fail(GN_ERR_EMPTY, "Index is empty — call set() first");
     if (k <= 0) return fail(GN_ERR_INVALID, "k must be positive");
     std::lock_guard<std::mutex> lk(ix->mu);
-    GN_TRY(ivfl2_search_dev(ix, d_queries, nq, (int)k, d_idx, d_dist, d_cnt, (cudaStream_t)stream));
+    IvfL2State &S = *ix->ivfl2;
+    if (S.graphs && nq > 0 && nq <= S.graphs->max_batch && k == S.graphs->k && !timing_on())
+        return ivfl2_search_graph(ix, d_queries, false, nq, (int)k, d_idx, d_dist, d_cnt, false, (cudaStream_t)stream);
+    const cudaStream_t st = (cudaStream_t)stream;
+    const float *dQ = d_queries;
+    if (S.d != S.dp) {  // kernels read queries at the padded pitch
+        GN_TRY(upload_rows(S.s.q, d_queries, nq, S.d * 4, S.dp / 4, st, true));
+        dQ = S.s.q.as<float>();
+    }
+    GN_TRY(ivfl2_search_core(ix, dQ, nq, (int)k, d_idx, d_dist, d_cnt, st));
     GN_CUDA_TRY(cudaGetLastError());
     return GN_OK;
 }
@@ -889,12 +900,14 @@ int gn_ivfl2_search_knn(gn_index *ix, const float *queries, int64_t nq, int64_t 
         return fail(GN_ERR_INVALID, "bad query arguments");
     std::lock_guard<std::mutex> lk(ix->mu);
     if (nq == 0) return GN_OK;
+    if (S.graphs && nq <= S.graphs->max_batch && k == S.graphs->k && !timing_on())
+        return ivfl2_search_graph(ix, queries, true, nq, (int)k, out_idx, out_dist, out_cnt, true, ix->stream);
     cudaStream_t st = ix->stream;
     GN_TRY(upload_rows(S.s.q, queries, nq, S.d * 4, S.dp / 4, st));
     GN_TRY(ix->out_idx.ensure((size_t)nq * k * 8));
     GN_TRY(ix->out_dist.ensure((size_t)nq * k * 4));
     GN_TRY(ix->part.ensure((size_t)nq * 8));
-    GN_TRY(ivfl2_search_dev(ix, S.s.q.as<float>(), nq, (int)k, ix->out_idx.as<int64_t>(), ix->out_dist.as<float>(),
+    GN_TRY(ivfl2_search_core(ix, S.s.q.as<float>(), nq, (int)k, ix->out_idx.as<int64_t>(), ix->out_dist.as<float>(),
                             ix->part.as<int64_t>(), st));
     GN_CUDA_TRY(cudaMemcpyAsync(out_idx, ix->out_idx.p, (size_t)nq * k * 8, cudaMemcpyDeviceToHost, st));
     GN_CUDA_TRY(cudaMemcpyAsync(out_dist, ix->out_dist.p, (size_t)nq * k * 4, cudaMemcpyDeviceToHost, st));
@@ -907,7 +920,9 @@ int gn_ivfl2_search_knn(gn_index *ix, const float *queries, int64_t nq, int64_t 
 int gn_ivfl2_set_n_probe(gn_index *ix, int32_t n_probe) {
     GN_TRY(ivfl2_check(ix));
     if (n_probe <= 0) return fail(GN_ERR_INVALID, "n_probe must be positive");
+    std::lock_guard<std::mutex> lk(ix->mu);
     ix->ivfl2->nprobe = n_probe;
+    ix->ivfl2->cfg++;
     return GN_OK;
 }
 

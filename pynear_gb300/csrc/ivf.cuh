@@ -37,6 +37,23 @@ struct IvfL2State {
     // learned probing (prober.cu): attached model and logit threshold
     gn_index *prober = nullptr;
     float prober_tau = 0.f;
+    // search configuration version (bumped by every setter); CUDA graphs
+    // captured for one configuration are replayed only under it
+    uint64_t cfg = 1;
+    struct IvfGraphs *graphs = nullptr;
+};
+
+// Captured batch pipelines of a float IVF index (ivf_graph.cu), one per batch
+// size, replayed on fixed staging buffers.
+struct IvfGraphs {
+    int64_t max_batch = 0;
+    int k = 0, dp = 0;
+    DBuf gq, gidx, gdist, gcnt;  // staging: queries (pitch dp), indices, distances, counts
+    std::vector<std::pair<int64_t, cudaGraphExec_t>> execs;  // batch size -> graph
+    uint64_t cfg = 0, gen = 0;
+    int64_t replays = 0, capture_failures = 0;
+    void clear();
+    ~IvfGraphs();
 };
 
 // Binary IVF (IVFFlatBinaryIndex semantics).
@@ -66,6 +83,11 @@ int ivfl2_coarse_run(gn_index *ix, const float *dQ, int64_t nq, int np, bool kee
                      cudaStream_t st);
 int ivfl2_coarse_sorted_keys(gn_index *ix, const float *dQ, int64_t nq, int np, uint64_t *keys, cudaStream_t st);
 int ivfl2_probes(gn_index *ix, const float *dQ, int64_t nq, int *np_out, cudaStream_t st);
+int ivfl2_search_core(gn_index *ix, const float *dQ, int64_t nq, int k, int64_t *d_idx, float *d_dist, int64_t *d_cnt,
+                      cudaStream_t st);
+// Graph-replayed search; queries/results on the host or the device.
+int ivfl2_search_graph(gn_index *ix, const float *q, bool q_host, int64_t nq, int k, int64_t *idx, float *dist,
+                       int64_t *cnt, bool out_host, cudaStream_t st);
 int ivfl2_search_tc(gn_index *ix, const float *dQ, int64_t nq, int k, int64_t *d_idx, float *d_dist, int64_t *d_cnt,
                     cudaStream_t st);
 int ivfl2_prepare_tc(gn_index *ix, cudaStream_t st);

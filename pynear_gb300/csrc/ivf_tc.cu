@@ -471,7 +471,8 @@ int ivfl2_search_tc(gn_index *ix, const float *dQ, int64_t nq, int k, int64_t *d
         S.q16.as<uint4>(), S.K / 8, np, T.bucket.as<int64_t>(), T.boff.as<int64_t>() + S.nc, T.qslot.as<int64_t>(),
         T.slot_rel.as<int64_t>(), S.qb.as<uint4>(), S.aslot.as<int64_t>(), npairs);
     const int64_t maxlen = S.top_rows.size() > 1 ? S.top_rows[1] : 0;
-    const int64_t max_units = (ceil_div(npairs, TC_QCHUNK) + S.nc) * (ceil_div(maxlen, rc) + 1);
+    // sized for the shortest row chunk (256) so that a smaller batch never needs more
+    const int64_t max_units = (ceil_div(npairs, TC_QCHUNK) + S.nc) * (ceil_div(maxlen, 256) + 1);
     GN_TRY(S.units.ensure((size_t)max_units * sizeof(TcUnit)));
     GN_TRY(S.nunits.ensure(8));
     tc_units_kernel<<<(unsigned)ceil_div(max_units, 256), 256, 0, st>>>(
@@ -528,6 +529,7 @@ extern "C" int gn_ivfl2_set_mode(gn_index *ix, int32_t mode, int32_t shortlist) 
     std::lock_guard<std::mutex> lk(ix->mu);
     ix->ivfl2->mode = mode;
     if (mode == 1) ix->ivfl2->shortlist = shortlist;
+    ix->ivfl2->cfg++;
     return GN_OK;
 }
 

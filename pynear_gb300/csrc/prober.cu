@@ -593,6 +593,7 @@ int gn_ivfl2_set_prober(gn_index *ivf, gn_index *pr, float logit_tau) {
     std::lock_guard<std::mutex> lk(ivf->mu);
     ivf->ivfl2->prober = pr;
     ivf->ivfl2->prober_tau = logit_tau;
+    ivf->ivfl2->cfg++;
     return GN_OK;
 }
 

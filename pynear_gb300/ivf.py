@@ -90,6 +90,18 @@ class IVFFlatL2Index:
         _lib.call("gn_ivfl2_set_prober", self._h.h, None if prober is None else prober._h.h,
                   prob_to_logit(threshold))
 
+    def enable_graphs(self, max_batch: int, k: int) -> None:
+        """Replay searches of 1..max_batch queries at this k as captured CUDA
+        graphs (one per batch size); max_batch 0 turns it off.  Results are
+        those of the uncaptured pipeline."""
+        _lib.call("gn_ivfl2_enable_graphs", self._h.h, int(max_batch), int(k))
+
+    def graph_info(self) -> dict:
+        out = np.zeros(4, np.int64)
+        _lib.call("gn_ivfl2_graph_info", self._h.h, _lib.ptr(out))
+        return {"max_batch": int(out[0]), "graphs": int(out[1]), "replays": int(out[2]),
+                "capture_failures": int(out[3])}
+
     def last_lists_probed(self, nq: int) -> np.ndarray:
         """Lists probed per query by the last search with a prober."""
         out = np.empty(nq, np.int32)
