@@ -52,6 +52,7 @@ struct IvfGraphs {
     std::vector<std::pair<int64_t, cudaGraphExec_t>> execs;  // batch size -> graph
     uint64_t cfg = 0, gen = 0;
     int64_t replays = 0, capture_failures = 0;
+    cudaEvent_t ev_in = nullptr, ev_out = nullptr;  // order the index's stream after / before the caller's
     void clear();
     ~IvfGraphs();
 };
@@ -87,7 +88,7 @@ int ivfl2_search_core(gn_index *ix, const float *dQ, int64_t nq, int k, int64_t 
                       cudaStream_t st);
 // Graph-replayed search; queries/results on the host or the device.
 int ivfl2_search_graph(gn_index *ix, const float *q, bool q_host, int64_t nq, int k, int64_t *idx, float *dist,
-                       int64_t *cnt, bool out_host, cudaStream_t st);
+                       int64_t *cnt, bool out_host, cudaStream_t user);
 int ivfl2_search_tc(gn_index *ix, const float *dQ, int64_t nq, int k, int64_t *d_idx, float *d_dist, int64_t *d_cnt,
                     cudaStream_t st);
 int ivfl2_prepare_tc(gn_index *ix, cudaStream_t st);

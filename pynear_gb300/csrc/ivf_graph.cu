@@ -26,6 +26,8 @@ void IvfGraphs::clear() {
 
 IvfGraphs::~IvfGraphs() {
     clear();
+    if (ev_in) cudaEventDestroy(ev_in);
+    if (ev_out) cudaEventDestroy(ev_out);
 }
 
 // Capture the pipeline for nq queries on st into an executable graph.
@@ -53,10 +55,18 @@ static int ivf_capture(gn_index *ix, int64_t nq, cudaStream_t st, cudaGraphExec_
     return GN_OK;
 }
 
+// Graphs are captured and replayed on the index's own (non-blocking) stream:
+// the caller's stream may be the legacy default stream, which cannot be
+// captured.  Events order the two streams both ways.
 int ivfl2_search_graph(gn_index *ix, const float *q, bool q_host, int64_t nq, int k, int64_t *idx, float *dist,
-                       int64_t *cnt, bool out_host, cudaStream_t st) {
+                       int64_t *cnt, bool out_host, cudaStream_t user) {
     IvfL2State &S = *ix->ivfl2;
     IvfGraphs &G = *S.graphs;
+    const cudaStream_t st = ix->stream;
+    if (user != st) {
+        GN_CUDA_TRY(cudaEventRecord(G.ev_in, user));
+        GN_CUDA_TRY(cudaStreamWaitEvent(st, G.ev_in, 0));
+    }
     if (G.dp != S.dp) {  // the data was replaced by rows of another width
         GN_TRY(G.gq.ensure((size_t)G.max_batch * S.dp * 4));
         GN_CUDA_TRY(cudaMemsetAsync(G.gq.p, 0, (size_t)G.max_batch * S.dp * 4, st));
@@ -102,7 +112,12 @@ int ivfl2_search_graph(gn_index *ix, const float *q, bool q_host, int64_t nq, in
     GN_CUDA_TRY(cudaMemcpyAsync(idx, G.gidx.p, (size_t)nq * k * 8, kout, st));
     GN_CUDA_TRY(cudaMemcpyAsync(dist, G.gdist.p, (size_t)nq * k * 4, kout, st));
     GN_CUDA_TRY(cudaMemcpyAsync(cnt, G.gcnt.p, (size_t)nq * 8, kout, st));
-    if (out_host) GN_CUDA_TRY(cudaStreamSynchronize(st));
+    if (out_host) {
+        GN_CUDA_TRY(cudaStreamSynchronize(st));
+    } else if (user != st) {
+        GN_CUDA_TRY(cudaEventRecord(G.ev_out, st));
+        GN_CUDA_TRY(cudaStreamWaitEvent(user, G.ev_out, 0));
+    }
     return GN_OK;
 }
 
@@ -132,6 +147,8 @@ extern "C" int gn_ivfl2_enable_graphs(gn_index *ix, int64_t max_batch, int32_t k
     G.k = k;
     G.dp = S.dp;
     G.replays = G.capture_failures = 0;
+    if (!G.ev_in) GN_CUDA_TRY(cudaEventCreateWithFlags(&G.ev_in, cudaEventDisableTiming));
+    if (!G.ev_out) GN_CUDA_TRY(cudaEventCreateWithFlags(&G.ev_out, cudaEventDisableTiming));
     GN_TRY(G.gq.ensure((size_t)max_batch * S.dp * 4));
     GN_TRY(G.gidx.ensure((size_t)max_batch * k * 8));
     GN_TRY(G.gdist.ensure((size_t)max_batch * k * 4));

@@ -89,7 +89,10 @@ def test_graph_replay_with_prober_and_rebuild(gn):
     assert ix.graph_info()["capture_failures"] == 0
 
 
-def test_graph_device_entry_point(gn):
+@pytest.mark.parametrize("side_stream", [True, False])
+def test_graph_device_entry_point(gn, side_stream):
+    # the caller's stream may be a side stream or the legacy default stream
+    # (which cannot be captured: the graphs run on the index's own stream)
     torch = pytest.importorskip("torch")
     from pynear_gb300 import _lib
 
@@ -100,7 +103,7 @@ def test_graph_device_entry_point(gn):
     ix.enable_graphs(256, 8)
     lib = _lib.load()
     dq = torch.from_numpy(q).cuda()
-    s = torch.cuda.Stream()
+    s = torch.cuda.Stream() if side_stream else torch.cuda.default_stream()
     s.wait_stream(torch.cuda.current_stream())
     for n in (256, 33, 256, 33):
         di = torch.empty((n, 8), dtype=torch.int64, device="cuda")
