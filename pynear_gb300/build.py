@@ -22,7 +22,7 @@ INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden",
-         "--expt-relaxed-constexpr", "-I" + INCLUDE]
+         "-Xcompiler", "-Werror=return-type", "--expt-relaxed-constexpr", "-I" + INCLUDE]
 
 
 def nvcc() -> str:

@@ -192,22 +192,32 @@ __global__ void ivf_bucket_fill_kernel(const int32_t *__restrict__ probes, int64
     if (l >= 0) bucket[boff[l] + atomicAdd(fill + l, 1)] = t;
 }
 
-// per query: slot offset of each probe (relative) and the query's slot count
+// per query (one warp): slot offset of each probe (relative, exclusive scan
+// of the probes' slot counts) and the query's slot count
 __global__ void ivf_slots_kernel(const int32_t *__restrict__ probes, int64_t nq, int np,
                                  const int64_t *__restrict__ list_off, int rc, int64_t *__restrict__ slot_rel,
                                  int64_t *__restrict__ qcount) {
-    const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane = threadIdx.x & 31;
+    const int64_t q = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     if (q >= nq) return;
     int64_t s = 0;
-    for (int p = 0; p < np; ++p) {
-        const int32_t l = probes[q * np + p];
-        slot_rel[q * np + p] = s;
-        if (l >= 0) {
-            const int64_t len = list_off[l + 1] - list_off[l];
-            s += (len + rc - 1) / rc;
+    for (int p0 = 0; p0 < np; p0 += 32) {
+        const int p = p0 + lane;
+        int64_t c = 0;
+        if (p < np) {
+            const int32_t l = probes[q * np + p];
+            if (l >= 0) c = (list_off[l + 1] - list_off[l] + rc - 1) / rc;
         }
+        int64_t inc = c;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int64_t v = __shfl_up_sync(0xffffffffu, inc, o);
+            if (lane >= o) inc += v;
+        }
+        if (p < np) slot_rel[q * np + p] = s + inc - c;
+        s += __shfl_sync(0xffffffffu, inc, 31);
     }
-    qcount[q] = s;
+    if (lane == 0) qcount[q] = s;
 }
 
 // qslot[0..nq] = exclusive scan of qcount (one block)
@@ -516,7 +526,7 @@ int ivf_plan(IvfScratch &S, int64_t nq, int np, int nc, const int64_t *d_list_of
                                         S.item_off.as<int64_t>());
     ivf_bucket_fill_kernel<<<pb, 256, 0, st>>>(S.probes.as<int32_t>(), npairs, S.boff.as<int64_t>(),
                                                S.fill.as<int32_t>(), S.bucket.as<int64_t>());
-    ivf_slots_kernel<<<(unsigned)ceil_div(nq, 128), 128, 0, st>>>(S.probes.as<int32_t>(), nq, np, d_list_off,
+    ivf_slots_kernel<<<(unsigned)ceil_div(nq, 4), 128, 0, st>>>(S.probes.as<int32_t>(), nq, np, d_list_off,
                                                                   slot_rc, S.slot_rel.as<int64_t>(),
                                                                   S.qcount.as<int64_t>());
     ivf_qscan_kernel<<<1, 1024, 0, st>>>(S.qcount.as<int64_t>(), nq, S.qslot.as<int64_t>());
@@ -881,7 +891,7 @@ int gn_ivfl2_search_knn_device(gn_index *ix, const float *d_queries, int64_t nq,
         return ivfl2_search_graph(ix, d_queries, false, nq, (int)k, d_idx, d_dist, d_cnt, false, (cudaStream_t)stream);
     const cudaStream_t st = (cudaStream_t)stream;
     const float *dQ = d_queries;
-    if (S.d != S.dp) {  // kernels read queries at the padded pitch
+    if (S.d != S.dp || ((uintptr_t)d_queries & 15)) {  // kernels read 16-byte aligned rows at the padded pitch
         GN_TRY(upload_rows(S.s.q, d_queries, nq, S.d * 4, S.dp / 4, st, true));
         dQ = S.s.q.as<float>();
     }

@@ -33,6 +33,7 @@ struct IvfL2State {
     int rc_tc = 4096;            // list rows per tensor-core work unit
     DBuf x16;                    // n*K BF16 rows, list order
     DBuf qb, aslot, units, nunits, err, scores;
+    DBuf sel_part, sel_done;     // split selection: partial best-S lists, per-query arrival counters
     DBuf q16, c16, cunits, cnunits, caslot, cscores;  // tensor-core coarse stage
     // learned probing (prober.cu): attached model and logit threshold
     gn_index *prober = nullptr;

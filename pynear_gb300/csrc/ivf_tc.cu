@@ -82,122 +82,469 @@ __global__ void tc_units_kernel(const int64_t *__restrict__ item_off, int nc, co
     units[i] = u;
 }
 
-// Squared L2 with a compensated FP32 sum: each (q_i - x_i)^2 is split into its
-// rounded product and the product's exact error (fma), the running sum keeps
-// its rounding error (two-sum); the errors are added back at the end.
-__device__ __forceinline__ float l2sq_compensated(const float *__restrict__ q, const float *__restrict__ x, int d) {
-    float s = 0.f, c = 0.f;
-    for (int i = 0; i < d; ++i) {
-        const float t = __fsub_rn(q[i], x[i]);
-        const float p = __fmul_rn(t, t);
-        const float e = __fmaf_rn(t, t, -p);
-        const float s2 = __fadd_rn(s, p);
-        const float bp = __fsub_rn(s2, s);
-        const float err = __fadd_rn(__fsub_rn(s, __fsub_rn(s2, bp)), __fsub_rn(p, bp));
+// Two-sum of a and b: s = fl(a + b) and its exact rounding error.
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
+    s = __fadd_rn(a, b);
+    const float bp = __fsub_rn(s, a);
+    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bp)), __fsub_rn(b, bp));
+}
+
+// Compensated accumulation of (a_i - b_i)^2 into (s, c): each square is split
+// into its rounded product and the product's exact error (fma), the running
+// sum keeps its rounding error (two-sum).
+__device__ __forceinline__ void l2_acc4(const float4 a, const float4 b, int valid, float &s, float &c) {
+    const float t[4] = {__fsub_rn(a.x, b.x), __fsub_rn(a.y, b.y), __fsub_rn(a.z, b.z), __fsub_rn(a.w, b.w)};
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+        if (u < valid) {
+            const float p = __fmul_rn(t[u], t[u]);
+            const float e = __fmaf_rn(t[u], t[u], -p);
+            float s2, err;
+            two_sum(s, p, s2, err);
+            s = s2;
+            c = __fadd_rn(c, __fadd_rn(err, e));
+        }
+    }
+}
+
+// Combine the 32 lanes' (sum, error) pairs with two-sums; the result is
+// within about one ulp of the exact sum.
+__device__ __forceinline__ float l2_warp_total(float s, float c) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const float so = __shfl_xor_sync(0xffffffffu, s, o), co = __shfl_xor_sync(0xffffffffu, c, o);
+        float s2, err;
+        two_sum(s, so, s2, err);
         s = s2;
-        c = __fadd_rn(c, __fadd_rn(err, e));
+        c = __fadd_rn(c, __fadd_rn(co, err));
     }
     return __fadd_rn(s, c);
 }
 
-// Selection over a query's score segments.  W warps share one query (W = 1
-// for large batches, up to 16 for small ones): warp w takes every W-th block
-// of 128 scores, keeps a register top-S, the partial lists meet in shared
-// memory and warp 0 merges them, re-ranks the S candidates exactly and writes
-// the k nearest.
-template <int RS>
-__global__ void ivf_tc_select_kernel(const float *__restrict__ scores, const int32_t *__restrict__ probes, int np,
-                                     const int64_t *__restrict__ qseg, const int64_t *__restrict__ seg_rel,
-                                     const int64_t *__restrict__ list_off, int S, const float *__restrict__ Q,
-                                     const float *__restrict__ X, int d, int dp, const int32_t *__restrict__ ids,
-                                     int64_t nq, int k, int W, int64_t *__restrict__ out_idx,
-                                     float *__restrict__ out_dist, int64_t *__restrict__ out_cnt) {
-    extern __shared__ uint64_t sel_smem[];  // [blockDim/32][32*RS] partial lists
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int qpb = (blockDim.x >> 5) / W;  // queries per block
-    const int64_t q = (int64_t)blockIdx.x * qpb + warp / W;
-    const int wq = warp % W;
-    const bool active = q < nq;
-    const float INF = __int_as_float(0x7f800000);
-    WarpTopK<RS> L;
-    L.init();
-    uint64_t thr = KEY_EMPTY;
-    float thr_f = INF;
-    if (active) {
-        int64_t blk = 0;  // running index of 256-score blocks over the query's segments
-        for (int p0 = 0; p0 < np; p0 += 32) {
-            // lane p holds probe p0 + p's list start, length and score segment
-            const int p = p0 + lane;
-            int64_t m_lb = 0, m_len = 0;
-            const float *m_sc = nullptr;
-            if (p < np) {
-                const int64_t pair = q * np + p;
-                const int32_t l = probes[pair];
-                if (l >= 0) {
-                    m_lb = list_off[l];
-                    m_len = list_off[l + 1] - m_lb;
-                    m_sc = scores + qseg[q] + seg_rel[pair];
+// Exact squared L2 (compensated FP32) of the query row q to rows[0..n) of X
+// (n <= 2), by one warp: lane l takes columns 4l..4l+3 of every 128-column
+// block (coalesced float4 loads, all of a 512-column block issued together).
+__device__ __forceinline__ void l2sq_warp_rows(const float *__restrict__ q, const float *__restrict__ X, int dp,
+                                               int d, const int64_t *rows, int n, float *out, int lane) {
+    float s[2] = {0.f, 0.f}, c[2] = {0.f, 0.f};
+    for (int base = 0; base < d; base += 512) {
+        float4 qa[4], xa[2][4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int i0 = base + u * 128 + lane * 4;
+            qa[u] = i0 < d ? *reinterpret_cast<const float4 *>(q + i0) : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+            for (int r = 0; r < 2; ++r)
+                xa[r][u] = (r < n && i0 < d) ? __ldg(reinterpret_cast<const float4 *>(X + rows[r] * dp + i0))
+                                             : make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int i0 = base + u * 128 + lane * 4;
+            const int valid = min(4, d - i0);
+#pragma unroll
+            for (int r = 0; r < 2; ++r)
+                if (r < n) l2_acc4(qa[u], xa[r][u], valid, s[r], c[r]);
+        }
+    }
+#pragma unroll
+    for (int r = 0; r < 2; ++r)
+        if (r < n) out[r] = l2_warp_total(s[r], c[r]);
+}
+
+// Ascending bitonic sort of n (power of two) keys in shared memory by the
+// whole block.
+template <int NT>
+__device__ __forceinline__ void block_bitonic_sort(uint64_t *a, int n) {
+    for (int size = 2; size <= n; size <<= 1)
+        for (int stride = size >> 1; stride > 0; stride >>= 1) {
+            for (int i = threadIdx.x; i < (n >> 1); i += NT) {
+                const int lo = 2 * i - (i & (stride - 1)), hi = lo + stride;
+                const bool asc = (lo & size) == 0;
+                const uint64_t x = a[lo], y = a[hi];
+                if ((x > y) == asc) {
+                    a[lo] = y;
+                    a[hi] = x;
                 }
             }
-            const int cnt = min(32, np - p0);
-            for (int pp = 0; pp < cnt; ++pp) {
-                const int64_t len = __shfl_sync(0xffffffffu, m_len, pp);
-                if (len == 0) continue;
-                const int64_t lb = __shfl_sync(0xffffffffu, m_lb, pp);
-                const float *sc = reinterpret_cast<const float *>(
-                    __shfl_sync(0xffffffffu, reinterpret_cast<uintptr_t>(m_sc), pp));
-                const int nblk = (int)((len + 255) / 256);
-                const int ilen = (int)len;
-                const int b0 = (int)((wq - blk % W + W) % W);  // first block of this segment owned by warp wq
-                for (int b = b0; b < nblk; b += W) {
-                    const int i0 = b * 256 + lane;
-                    float v[8];
+            __syncthreads();
+        }
+}
+
+constexpr int SEL_PCH = 256;   // probes staged per pass
+constexpr int SEL_EPT = 16;    // scores per lane per warp chunk (chunk = 512 scores)
+constexpr int SEL_WB = 512;    // candidate keys buffered per warp
+
+// Ascending bitonic sort of n (power of two, <= 512) keys in shared memory by
+// one warp.
+__device__ __forceinline__ void warp_bitonic_sort(uint64_t *a, int n, int lane) {
+    for (int size = 2; size <= n; size <<= 1)
+        for (int stride = size >> 1; stride > 0; stride >>= 1) {
+            for (int i = lane; i < (n >> 1); i += 32) {
+                const int lo = 2 * i - (i & (stride - 1)), hi = lo + stride;
+                const bool asc = (lo & size) == 0;
+                const uint64_t x = a[lo], y = a[hi];
+                if ((x > y) == asc) {
+                    a[lo] = y;
+                    a[hi] = x;
+                }
+            }
+            __syncwarp();
+        }
+}
+
+// The S smallest of a key multiset held in shared memory, by the whole block
+// (radix select on 8-bit digits from the top, stopping as soon as the
+// boundary digit is taken whole).  The keys are keys[w * WB + i], i < cnt[w],
+// one region per warp (warp w reads region w).  The S smallest (all, if
+// fewer) go to out[], in no particular order; returns how many.  Keys are
+// unique, so exactly min(S, total) are selected.
+template <int NT>
+__device__ int block_radix_select(const uint64_t *keys, int WB, const int *cnt, int S, uint64_t *out, int *hist,
+                                  int *sh) {
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    const uint64_t *mine = keys + (size_t)warp * WB;
+    const int nmine = cnt[warp];
+    uint64_t prefix = 0, mask = 0;
+    int need = S;
+    bool all = false;  // keys matching the prefix are all taken
+    for (int shift = 56; shift >= 0; shift -= 8) {
+        for (int i = t; i < 256; i += NT) hist[i] = 0;
+        __syncthreads();
+        for (int i = lane; i < nmine; i += 32) {
+            const uint64_t k = mine[i];
+            if ((k & mask) == prefix) atomicAdd(&hist[(k >> shift) & 255], 1);
+        }
+        __syncthreads();
+        if (warp == 0) {
+            int h[8], sum = 0;
 #pragma unroll
-                    for (int u = 0; u < 8; ++u) v[u] = (i0 + u * 32 < ilen) ? __ldg(sc + i0 + u * 32) : INF;
-                    float m = v[0];
+            for (int e = 0; e < 8; ++e) {
+                h[e] = hist[lane * 8 + e];
+                sum += h[e];
+            }
+            int inc = sum;
 #pragma unroll
-                    for (int u = 1; u < 8; ++u) m = fminf(m, v[u]);
-                    if (!__any_sync(0xffffffffu, m <= thr_f)) continue;
+            for (int o = 1; o < 32; o <<= 1) {
+                const int v = __shfl_up_sync(0xffffffffu, inc, o);
+                if (lane >= o) inc += v;
+            }
+            int before = inc - sum;
 #pragma unroll
-                    for (int u = 0; u < 8; ++u) {
-                        const int i = i0 + u * 32;
-                        const uint64_t key = (i < ilen) ? make_key(f2ord(v[u]), (uint32_t)(lb + i)) : KEY_EMPTY;
-                        L.offer(key, thr, S);
-                        thr_f = (thr == KEY_EMPTY) ? INF : ord2f(key_dist(thr));
+            for (int e = 0; e < 8; ++e) {
+                if (before < need && need <= before + h[e]) {
+                    sh[0] = lane * 8 + e;
+                    sh[1] = before;
+                }
+                before += h[e];
+            }
+            if (lane == 31) sh[2] = inc;  // keys matching the prefix
+        }
+        __syncthreads();
+        if (shift == 56 && sh[2] <= S) {  // no more keys than S: take them all
+            all = true;
+            break;
+        }
+        const int dg = sh[0];
+        need -= sh[1];
+        prefix |= (uint64_t)dg << shift;
+        mask |= (uint64_t)0xff << shift;
+        const bool whole = hist[dg] == need;
+        __syncthreads();
+        if (whole) {
+            all = true;
+            break;
+        }
+    }
+    // take every key below the prefix and the keys equal to it (all of them,
+    // or the single key left after all eight digits)
+    if (t == 0) sh[3] = 0;
+    __syncthreads();
+    for (int i = lane; i < nmine; i += 32) {
+        const uint64_t k = mine[i];
+        const uint64_t km = k & mask;
+        if (km < prefix || (km == prefix && (all || need > 0))) out[atomicAdd(&sh[3], 1)] = k;
+    }
+    __syncthreads();
+    return sh[3];
+}
+
+// Selection of one query by B blocks of 256 threads (B = 1 for large batches;
+// small batches split each query's range over up to 16 blocks, whose partial
+// best-S lists the last block to finish merges).  The query's score segments
+// (one per probed list, in probe order) form one flat range, swept in chunks
+// of 512 scores, chunk c by warp c mod 8, 16 coalesced loads per lane in
+// flight.  Keys are (score, row), so ties go to the lower row.
+//   threshold  from the block's first 8 chunks: a 256-bin histogram of their
+//              ordered score bits over [min, max]; the upper edge of the bin
+//              holding their S-th smallest is an upper bound of the query's
+//              S-th best score;
+//   filter     a score passes if it is not above the thresholds, so almost
+//              every chunk is rejected by one compare per score and one vote
+//              per warp;
+//   buffer     passing keys go to the warp's own shared-memory buffer (512
+//              keys); a full buffer is sorted and cut to its best S, which
+//              lowers the warp's threshold and the block's;
+//   select     radix select of the S smallest keys of all warps' buffers;
+//   re-rank    warp per candidate: exact squared L2 in FP32 (compensated sum);
+//              warp 0 returns the k nearest, ties to the lower original index.
+// No block barrier runs inside the sweep.
+template <int NT>
+__global__ void __launch_bounds__(NT, 1024 / NT) ivf_tc_select_kernel(
+    const float *__restrict__ scores, const int32_t *__restrict__ probes, int np, const int64_t *__restrict__ qseg,
+    const int64_t *__restrict__ seg_rel, const int64_t *__restrict__ list_off, int S, const float *__restrict__ Q,
+    const float *__restrict__ X, int d, int dp, const int32_t *__restrict__ ids, int64_t nq, int k, int B,
+    uint64_t *__restrict__ part, int *__restrict__ done, int64_t *__restrict__ out_idx, float *__restrict__ out_dist,
+    int64_t *__restrict__ out_cnt) {
+    constexpr int NW = NT / 32;
+    constexpr int CH = 32 * SEL_EPT;
+    __shared__ uint64_t wreg[NW * SEL_WB];
+    __shared__ int64_t p_seg[SEL_PCH], p_lb[SEL_PCH], p_pre[SEL_PCH + 1];
+    __shared__ int64_t w_sum[NW];
+    __shared__ uint64_t sel[64], s_rk[64];
+    __shared__ int hist[256], sh[4], s_wn[NW];
+    __shared__ unsigned long long s_thr;
+    __shared__ unsigned int s_u[2];
+    __shared__ int s_nv, s_last;
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    const int64_t q = blockIdx.x / B;
+    const int bq = (int)(blockIdx.x % B);  // this block's share of the query's range (B > 1 needs np <= SEL_PCH)
+    uint64_t *W = wreg + warp * SEL_WB;
+    if (t == 0) s_thr = KEY_EMPTY;
+    __syncthreads();
+    int wn = 0;                 // keys in this warp's buffer (warp-uniform)
+    uint64_t wthr = KEY_EMPTY;  // this warp's threshold
+
+    for (int p0 = 0; p0 < np; p0 += SEL_PCH) {
+        const int pc = min(SEL_PCH, np - p0);
+        // per-probe metadata and the prefix sum of the segment lengths
+        int64_t len = 0;
+        if (t < pc) {
+            const int64_t pair = q * np + p0 + t;
+            const int32_t l = probes[pair];
+            if (l >= 0) {
+                p_lb[t] = list_off[l];
+                len = list_off[l + 1] - p_lb[t];
+                p_seg[t] = qseg[q] + seg_rel[pair];
+            } else {
+                p_lb[t] = 0;
+                p_seg[t] = 0;
+            }
+        }
+        int64_t inc = len;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int64_t v = __shfl_up_sync(0xffffffffu, inc, o);
+            if (lane >= o) inc += v;
+        }
+        if (lane == 31) w_sum[warp] = inc;
+        __syncthreads();
+        int64_t before = 0;
+        for (int w = 0; w < warp; ++w) before += w_sum[w];
+        if (t < pc) p_pre[t + 1] = before + inc;
+        if (t == 0) p_pre[0] = 0;
+        __syncthreads();
+        const int64_t all = p_pre[pc];
+        const int64_t lo = all * bq / B, hi = all * (bq + 1) / B;
+        int pw = 0;  // probe of the chunk start (monotone over the warp's chunks)
+        uint32_t v[SEL_EPT];  // ordered score bits (f2ord)
+        uint32_t valid = 0;
+        bool full = false;
+        // chunk [c0, min(c0 + 512, hi)) into v[] (lane l: scores c0 + 32 j + l)
+        auto load = [&](int64_t c0) {
+            const int64_t cend = min(c0 + CH, hi);
+            while (p_pre[pw + 1] <= c0) ++pw;
+            const bool one = cend <= p_pre[pw + 1];  // chunk inside one segment
+            full = cend - c0 == CH;
+            if (one && full) {
+                const float *src = scores + p_seg[pw] + (c0 - p_pre[pw]) + lane;
+#pragma unroll
+                for (int j = 0; j < SEL_EPT; ++j) v[j] = f2ord(__ldg(src + j * 32));
+                valid = 0xffffu;
+            } else {
+                valid = 0;
+#pragma unroll
+                for (int j = 0; j < SEL_EPT; ++j) {
+                    const int64_t f = c0 + j * 32 + lane;
+                    v[j] = 0xffffffffu;
+                    if (f < cend) {
+                        int p = pw;
+                        while (p_pre[p + 1] <= f) ++p;
+                        v[j] = f2ord(__ldg(scores + p_seg[p] + (f - p_pre[p])));
+                        valid |= 1u << j;
                     }
                 }
-                blk += nblk;
             }
-        }
-    }
-    if (W > 1) {
-        uint64_t *mine = sel_smem + (size_t)warp * 32 * RS;
+        };
+        int64_t c0 = lo + (int64_t)warp * CH;
+        if (c0 < hi) load(c0);
+        if (p0 == 0) {
+            // block threshold from the block's first 8 chunks: an upper
+            // bound of their S-th smallest score, hence of the query's
+            uint32_t mn = 0xffffffffu, mx = 0;
 #pragma unroll
-        for (int r = 0; r < RS; ++r) mine[r * 32 + lane] = L.v[r];
+            for (int j = 0; j < SEL_EPT; ++j) {
+                if ((valid >> j) & 1u) {
+                    mn = min(mn, v[j]);
+                    mx = max(mx, v[j]);
+                }
+            }
+            mn = __reduce_min_sync(0xffffffffu, mn);
+            mx = __reduce_max_sync(0xffffffffu, mx);
+            const int nv = __reduce_add_sync(0xffffffffu, __popc(valid));
+            if (t == 0) {
+                s_u[0] = 0xffffffffu;
+                s_u[1] = 0;
+                s_nv = 0;
+            }
+            for (int i = t; i < 256; i += NT) hist[i] = 0;
+            __syncthreads();
+            if (lane == 0) {
+                atomicMin(&s_u[0], mn);
+                atomicMax(&s_u[1], mx);
+                atomicAdd(&s_nv, nv);
+            }
+            __syncthreads();
+            if (s_nv >= S) {
+                // 256-bin histogram of the sample over [min, max]; the upper
+                // edge of the bin holding the S-th smallest bounds it
+                const uint32_t lo_o = s_u[0], range = s_u[1] - lo_o;
+                const int sh_b = max(0, 24 - __clz(range | 1));  // (range >> sh_b) < 256
+#pragma unroll
+                for (int j = 0; j < SEL_EPT; ++j)
+                    if ((valid >> j) & 1u) atomicAdd(&hist[(v[j] - lo_o) >> sh_b], 1);
+                __syncthreads();
+                if (warp == 0) {
+                    int h[8], sum = 0;
+#pragma unroll
+                    for (int e = 0; e < 8; ++e) {
+                        h[e] = hist[lane * 8 + e];
+                        sum += h[e];
+                    }
+                    int inc = sum;
+#pragma unroll
+                    for (int o = 1; o < 32; o <<= 1) {
+                        const int x = __shfl_up_sync(0xffffffffu, inc, o);
+                        if (lane >= o) inc += x;
+                    }
+                    int before = inc - sum;
+#pragma unroll
+                    for (int e = 0; e < 8; ++e) {
+                        if (before < S && S <= before + h[e]) {
+                            const uint64_t edge = (uint64_t)lo_o + ((uint64_t)(lane * 8 + e + 1) << sh_b) - 1;
+                            s_thr = make_key((uint32_t)min(edge, (uint64_t)s_u[1]), 0xffffffffu);
+                        }
+                        before += h[e];
+                    }
+                }
+            }
+            __syncthreads();
+            wthr = s_thr;
+        }
+        while (c0 < hi) {
+            uint64_t thr = min(wthr, (uint64_t)*reinterpret_cast<volatile unsigned long long *>(&s_thr));
+            const uint32_t thr_o = key_dist(thr);
+            uint32_t pend = 0;
+#pragma unroll
+            for (int j = 0; j < SEL_EPT; ++j) pend |= (v[j] <= thr_o ? 1u : 0u) << j;
+            pend &= valid;
+            uint32_t wpend = __reduce_or_sync(0xffffffffu, pend);  // positions pending in some lane
+            while (wpend) {
+#pragma unroll
+                for (int j = 0; j < SEL_EPT; ++j) {
+                    if (!((wpend >> j) & 1u)) continue;  // warp-uniform
+                    bool want = (pend >> j) & 1u;
+                    uint64_t key = KEY_EMPTY;
+                    if (want) {
+                        const int64_t f = c0 + j * 32 + lane;
+                        int p = pw;
+                        while (p_pre[p + 1] <= f) ++p;
+                        key = make_key(v[j], (uint32_t)(p_lb[p] + (f - p_pre[p])));
+                        want = key < thr;
+                        if (!want) pend &= ~(1u << j);
+                    }
+                    const unsigned bal = __ballot_sync(0xffffffffu, want);
+                    if (bal) {
+                        const int pos = wn + __popc(bal & ((1u << lane) - 1u));
+                        if (want && pos < SEL_WB) {
+                            W[pos] = key;
+                            pend &= ~(1u << j);
+                        }
+                        wn += __popc(bal);
+                    }
+                }
+                if (wn <= SEL_WB) break;
+                // full: keep the best S, keys that did not fit are offered again
+                __syncwarp();
+                warp_bitonic_sort(W, SEL_WB, lane);
+                wthr = W[S - 1];
+                if (lane == 0) atomicMin(&s_thr, (unsigned long long)wthr);
+                wn = S;
+                thr = min(wthr, (uint64_t)*reinterpret_cast<volatile unsigned long long *>(&s_thr));
+                wpend = __reduce_or_sync(0xffffffffu, pend);
+                __syncwarp();
+            }
+            c0 += (int64_t)NW * CH;
+            if (c0 < hi) load(c0);
+        }
         __syncthreads();
-        if (wq == 0 && active) {
-            for (int w = 1; w < W; ++w) {
-                const uint64_t *other = sel_smem + (size_t)(warp + w) * 32 * RS;
-#pragma unroll
-                for (int r = 0; r < RS; ++r) L.offer(other[r * 32 + lane], thr, S);
-            }
-        }
     }
-    if (!active || wq != 0) return;
+    if (lane == 0) s_wn[warp] = wn;
+    __syncthreads();
+    int m = block_radix_select<NT>(wreg, SEL_WB, s_wn, S, sel, hist, sh);
+    if (B > 1) {
+        // publish this block's best S; the last block of the query merges all
+        uint64_t *mine = part + ((size_t)q * B + bq) * S;
+        for (int i = t; i < S; i += NT) mine[i] = i < m ? sel[i] : KEY_EMPTY;
+        __threadfence();
+        __syncthreads();
+        if (t == 0) s_last = atomicAdd(done + q, 1) == B - 1;
+        __syncthreads();
+        if (!s_last) return;
+        __threadfence();
+        // block b's list goes to region b mod 8 (at offset (b / 8) * S)
+        const uint64_t *all_q = part + (size_t)q * B * S;
+        for (int i = t; i < B * S; i += NT) {
+            const int b = i / S;
+            wreg[(b % NW) * SEL_WB + (b / NW) * S + i % S] = __ldcg(all_q + i);
+        }
+        if (t < NW) s_wn[t] = ((B - t + NW - 1) / NW) * S;
+        if (t == 0) done[q] = 0;  // ready for the next batch
+        __syncthreads();
+        m = block_radix_select<NT>(wreg, SEL_WB, s_wn, S, sel, hist, sh);
+    }
+
+    // exact re-rank of the candidates, two rows per warp at a time
+    const float *qrow = Q + q * dp;
+    for (int r = 2 * warp; r < S; r += 2 * NW) {
+        int64_t rows[2];
+        int n = 0;
+        for (int u = 0; u < 2; ++u) {
+            const uint64_t c = (r + u < S && r + u < m) ? sel[r + u] : KEY_EMPTY;
+            rows[u] = c != KEY_EMPTY ? (int64_t)key_idx(c) : -1;
+        }
+        n = rows[0] < 0 ? 0 : (rows[1] < 0 ? 1 : 2);
+        if (rows[0] < 0 && rows[1] >= 0) {  // keep the valid row first
+            rows[0] = rows[1];
+            rows[1] = -1;
+            n = 1;
+        }
+        float dd[2];
+        if (n) l2sq_warp_rows(qrow, X, dp, d, rows, n, dd, lane);
+        if (lane == 0)
+            for (int u = 0; u < 2 && r + u < S; ++u) s_rk[r + u] = KEY_EMPTY;
+        __syncwarp();
+        if (lane == 0)
+            for (int u = 0; u < n; ++u) s_rk[r + u] = make_key(__float_as_uint(dd[u]), (uint32_t)ids[rows[u]]);
+    }
+    __syncthreads();
+    if (warp != 0) return;
     WarpTopK<1> F;
     F.init();
     uint64_t fthr = KEY_EMPTY;
-#pragma unroll
-    for (int r = 0; r < RS; ++r) {
-        const int pos = r * 32 + lane;
-        const uint64_t key = L.v[r];
-        uint64_t fk = KEY_EMPTY;
-        if (pos < S && key != KEY_EMPTY) {
-            const int64_t row = key_idx(key);
-            const float dd = l2sq_compensated(Q + q * dp, X + row * dp, d);
-            fk = make_key(__float_as_uint(dd), (uint32_t)ids[row]);
-        }
-        F.offer(fk, fthr, k);
+    for (int r0 = 0; r0 < S; r0 += 32) {
+        const uint64_t key = (r0 + lane < S) ? s_rk[r0 + lane] : KEY_EMPTY;
+        F.offer(key, fthr, k);
     }
     const uint64_t key = F.v[0];
     const bool e = key == KEY_EMPTY;
@@ -324,30 +671,57 @@ __global__ void __launch_bounds__(256) coarse_probe_kernel(const float *__restri
     const __nv_bfloat16 *W1 = reinterpret_cast<const __nv_bfloat16 *>(w.W1);
     const __nv_bfloat16 *W2 = reinterpret_cast<const __nv_bfloat16 *>(w.W2);
     const __nv_bfloat16 *W3 = reinterpret_cast<const __nv_bfloat16 *>(w.W3);
+    // layer 1: thread j = hidden unit j, gathered rows of W1 (loads issued ahead)
     float a = w.b1[j];
-    for (int i = 0; i < NC; ++i)
-        if (sc[i] >= 0) a = fmaf(sf[i], __bfloat162float(W1[(size_t)sc[i] * H + j]), a);
+#pragma unroll 16
+    for (int i = 0; i < NC; ++i) {
+        const int c = sc[i];
+        const float wv = c >= 0 ? __bfloat162float(W1[(size_t)c * H + j]) : 0.f;
+        a = fmaf(sf[i], wv, a);
+    }
     sh1[j] = fmaxf(a, 0.f);
     __syncthreads();
-    for (int o = warp * 32; o < warp * 32 + 32; ++o) {
-        float s = 0.f;
+    // layer 2: thread j = output j, its W2 row in 16-byte loads
+    {
+        const uint4 *row = reinterpret_cast<const uint4 *>(W2 + (size_t)j * H);
+        float acc[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll 8
+        for (int v = 0; v < H / 8; ++v) {
+            const uint4 u = __ldg(row + v);
+            const __nv_bfloat162 *h = reinterpret_cast<const __nv_bfloat162 *>(&u);
 #pragma unroll
-        for (int k = lane; k < H; k += 32) s = fmaf(__bfloat162float(W2[(size_t)o * H + k]), sh1[k], s);
-#pragma unroll
-        for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
-        if (lane == 0) sh2[o] = fmaxf(s + w.b2[o], 0.f);
+            for (int e = 0; e < 4; ++e) {
+                const float2 f = __bfloat1622float2(h[e]);
+                acc[e] = fmaf(f.x, sh1[v * 8 + 2 * e], acc[e]);
+                acc[e] = fmaf(f.y, sh1[v * 8 + 2 * e + 1], acc[e]);
+            }
+        }
+        sh2[j] = fmaxf((acc[0] + acc[1]) + (acc[2] + acc[3]) + w.b2[j], 0.f);
     }
     __syncthreads();
-    for (int i = warp; i < NC; i += 8) {
+    // layer 3: 4 threads per candidate, 64 hidden units each
+    {
+        const int i = j >> 2, part = j & 3;
         const int c = sc[i];
-        float s = 0.f;
+        float acc = 0.f;
         if (c >= 0) {
+            const uint4 *row = reinterpret_cast<const uint4 *>(W3 + (size_t)c * H + part * (H / 4));
 #pragma unroll
-            for (int k = lane; k < H; k += 32) s = fmaf(__bfloat162float(W3[(size_t)c * H + k]), sh2[k], s);
+            for (int v = 0; v < H / 32; ++v) {
+                const uint4 u = __ldg(row + v);
+                const __nv_bfloat162 *h = reinterpret_cast<const __nv_bfloat162 *>(&u);
 #pragma unroll
-            for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
+                for (int e = 0; e < 4; ++e) {
+                    const float2 f = __bfloat1622float2(h[e]);
+                    const int kk = part * (H / 4) + v * 8 + 2 * e;
+                    acc = fmaf(f.x, sh2[kk], acc);
+                    acc = fmaf(f.y, sh2[kk + 1], acc);
+                }
+            }
         }
-        if (lane == 0) sz[i] = c >= 0 ? s + w.b3[c] : -INFINITY;
+        acc += __shfl_xor_sync(0xffffffffu, acc, 1);
+        acc += __shfl_xor_sync(0xffffffffu, acc, 2);
+        if (part == 0) sz[i] = c >= 0 ? acc + w.b3[c] : -INFINITY;
     }
     __syncthreads();
     bool keep = false;
@@ -497,22 +871,36 @@ int ivfl2_search_tc(gn_index *ix, const float *dQ, int64_t nq, int k, int64_t *d
     timing_begin(st, "tc_ivf_kernel");
     GN_TRY(tc_ivf_launch(a, st));
     timing_end(st);
-    // warps per query: enough warps in flight for small batches
-    int W = 1;
-    while (W < 16 && nq * W <= (int64_t)dev_info().num_sms * 64) W *= 2;
-    const int qpb = std::max(1, 8 / W);
-    const int threads = 32 * W * qpb;
-    const unsigned blocks = (unsigned)ceil_div(nq, qpb);
-    auto sel = [&](auto RC) {
-        constexpr int R = decltype(RC)::value;
-        const size_t smem = W > 1 ? (size_t)(threads / 32) * 32 * R * 8 : 0;
-        ivf_tc_select_kernel<R><<<blocks, threads, smem, st>>>(
+    // B blocks per query: split small batches so that they still fill the GPU
+    const int nsm = dev_info().num_sms;
+    int B = 1;
+    if (np <= SEL_PCH)
+        while (B < 16 && nq * B * 2 <= (int64_t)nsm * 4) B *= 2;
+    if (B > 1) {
+        // nq * B <= 4 * SMs here: one size for every small batch
+        GN_TRY(S.sel_part.ensure((size_t)std::max<int64_t>(nq * B, (int64_t)nsm * 4) * S.shortlist * 8));
+        const size_t cap0 = S.sel_done.cap;
+        GN_TRY(S.sel_done.ensure((size_t)std::max<int64_t>(nq, 1024) * 4));
+        if (S.sel_done.cap != cap0) GN_CUDA_TRY(cudaMemsetAsync(S.sel_done.p, 0, S.sel_done.cap, st));
+    }
+    const unsigned blocks = (unsigned)(nq * B);
+    // small batches: 8 warps per query part; large: 4 warps, more queries in flight
+    auto sel = [&](auto NTC) -> int {
+        constexpr int NT = decltype(NTC)::value;
+        static bool carve = false;  // shared memory over L1: the scores are streamed once
+        if (!carve) {
+            GN_CUDA_TRY(cudaFuncSetAttribute(ivf_tc_select_kernel<NT>,
+                                             cudaFuncAttributePreferredSharedMemoryCarveout, 100));
+            carve = true;
+        }
+        ivf_tc_select_kernel<NT><<<blocks, NT, 0, st>>>(
             S.scores.as<float>(), T.probes.as<int32_t>(), np, T.qslot.as<int64_t>(), T.slot_rel.as<int64_t>(),
-            S.list_off.as<int64_t>(), S.shortlist, dQ, S.vecs.as<float>(), S.d, S.dp, S.ids.as<int32_t>(), nq, k, W,
-            d_idx, d_dist, d_cnt);
+            S.list_off.as<int64_t>(), S.shortlist, dQ, S.vecs.as<float>(), S.d, S.dp, S.ids.as<int32_t>(), nq, k, B,
+            S.sel_part.as<uint64_t>(), S.sel_done.as<int>(), d_idx, d_dist, d_cnt);
+        return GN_OK;
     };
-    if (S.shortlist <= 32) sel(std::integral_constant<int, 1>());
-    else sel(std::integral_constant<int, 2>());
+    if (nq * B >= (int64_t)nsm * 8) GN_TRY(sel(std::integral_constant<int, 128>()));
+    else GN_TRY(sel(std::integral_constant<int, 256>()));
     GN_CUDA_TRY(cudaGetLastError());
     return GN_OK;
 }
