@@ -450,16 +450,20 @@ __global__ void __launch_bounds__(NT, 1024 / NT) ivf_tc_select_kernel(
             pend &= valid;
             uint32_t wpend = __reduce_or_sync(0xffffffffu, pend);  // positions pending in some lane
             while (wpend) {
+                // one position at a time (warp-uniform); the body is not
+                // unrolled, to keep the kernel small for the instruction cache
+                for (uint32_t bits = wpend; bits; bits &= bits - 1) {
+                    const int j = __ffs(bits) - 1;
+                    uint32_t vj = 0;
 #pragma unroll
-                for (int j = 0; j < SEL_EPT; ++j) {
-                    if (!((wpend >> j) & 1u)) continue;  // warp-uniform
+                    for (int jj = 0; jj < SEL_EPT; ++jj) vj = jj == j ? v[jj] : vj;
                     bool want = (pend >> j) & 1u;
                     uint64_t key = KEY_EMPTY;
                     if (want) {
                         const int64_t f = c0 + j * 32 + lane;
                         int p = pw;
                         while (p_pre[p + 1] <= f) ++p;
-                        key = make_key(v[j], (uint32_t)(p_lb[p] + (f - p_pre[p])));
+                        key = make_key(vj, (uint32_t)(p_lb[p] + (f - p_pre[p])));
                         want = key < thr;
                         if (!want) pend &= ~(1u << j);
                     }
@@ -591,28 +595,25 @@ __global__ void __launch_bounds__(256) coarse_probe_kernel(const float *__restri
                                                            int32_t *__restrict__ nprobed) {
     constexpr int NC = PROBER_CAND, H = PROBER_HIDDEN;
     __shared__ int32_t sc[NC];
-    __shared__ float sd[NC], sf[NC], sh1[H], sh2[H], sz[NC];
+    __shared__ float sd[NC], sf[NC], sz[NC];
+    __shared__ __align__(16) float sh1[H], sh2[H];
     __shared__ int s_cnt0;
     __shared__ __align__(16) float sqr[PROBE_MAX_D];
-    extern __shared__ uint64_t skeys[];  // next_pow2(nc) keys
+    __shared__ int hist[256], rsh[4], rcnt[8];
+    __shared__ uint64_t top[NC];
+    extern __shared__ uint64_t skeys[];  // next_pow2(nc) keys, 8 regions of next_pow2(nc) / 8
     const int64_t q = blockIdx.x;
     const int j = threadIdx.x, lane = j & 31, warp = j >> 5;
     const float *sq = scores + q * nc;
     for (int t = j; t < d; t += 256) sqr[t] = Q[q * dp + t];
-    // block-wide bitonic sort of the BF16 scores; the first 64 are the candidates
-    for (int c = j; c < ncp2; c += 256) skeys[c] = c < nc ? make_key(f2ord(sq[c]), (uint32_t)c) : KEY_EMPTY;
+    // the 64 smallest keys (BF16 score, centroid) are the candidates: radix
+    // select over the 8 warps' regions
+    const int wb = ncp2 >> 3;
+    for (int c = j; c < nc; c += 256) skeys[c] = make_key(f2ord(sq[c]), (uint32_t)c);
+    if (j < 8) rcnt[j] = max(0, min(wb, nc - j * wb));
     __syncthreads();
-    for (int size = 2; size <= ncp2; size <<= 1)
-        for (int stride = size >> 1; stride > 0; stride >>= 1) {
-            for (int i = j; i < ncp2 / 2; i += 256) {
-                const int lo = 2 * i - (i & (stride - 1)), hi = lo + stride;
-                const bool up = (lo & size) == 0;
-                const uint64_t a = skeys[lo], b = skeys[hi];
-                if ((a > b) == up) { skeys[lo] = b; skeys[hi] = a; }
-            }
-            __syncthreads();
-        }
-    if (j < NC) sc[j] = skeys[j] == KEY_EMPTY ? -1 : (int32_t)key_idx(skeys[j]);
+    const int ntop = block_radix_select<256>(skeys, wb, rcnt, NC, top, hist, rsh);
+    if (j < NC) sc[j] = j < ntop ? (int32_t)key_idx(top[j]) : -1;
     __syncthreads();
     {   // exact squared distances: 4 threads per candidate, float4 strides
         const int i = j >> 2, part = j & 3;
@@ -684,16 +685,19 @@ __global__ void __launch_bounds__(256) coarse_probe_kernel(const float *__restri
     // layer 2: thread j = output j, its W2 row in 16-byte loads
     {
         const uint4 *row = reinterpret_cast<const uint4 *>(W2 + (size_t)j * H);
+        const float4 *h4 = reinterpret_cast<const float4 *>(sh1);
         float acc[4] = {0.f, 0.f, 0.f, 0.f};
 #pragma unroll 8
         for (int v = 0; v < H / 8; ++v) {
             const uint4 u = __ldg(row + v);
             const __nv_bfloat162 *h = reinterpret_cast<const __nv_bfloat162 *>(&u);
+            const float4 x0 = h4[2 * v], x1 = h4[2 * v + 1];
+            const float xs[8] = {x0.x, x0.y, x0.z, x0.w, x1.x, x1.y, x1.z, x1.w};
 #pragma unroll
             for (int e = 0; e < 4; ++e) {
                 const float2 f = __bfloat1622float2(h[e]);
-                acc[e] = fmaf(f.x, sh1[v * 8 + 2 * e], acc[e]);
-                acc[e] = fmaf(f.y, sh1[v * 8 + 2 * e + 1], acc[e]);
+                acc[e] = fmaf(f.x, xs[2 * e], acc[e]);
+                acc[e] = fmaf(f.y, xs[2 * e + 1], acc[e]);
             }
         }
         sh2[j] = fmaxf((acc[0] + acc[1]) + (acc[2] + acc[3]) + w.b2[j], 0.f);
@@ -706,16 +710,18 @@ __global__ void __launch_bounds__(256) coarse_probe_kernel(const float *__restri
         float acc = 0.f;
         if (c >= 0) {
             const uint4 *row = reinterpret_cast<const uint4 *>(W3 + (size_t)c * H + part * (H / 4));
+            const float4 *h4 = reinterpret_cast<const float4 *>(sh2 + part * (H / 4));
 #pragma unroll
             for (int v = 0; v < H / 32; ++v) {
                 const uint4 u = __ldg(row + v);
                 const __nv_bfloat162 *h = reinterpret_cast<const __nv_bfloat162 *>(&u);
+                const float4 x0 = h4[2 * v], x1 = h4[2 * v + 1];
+                const float xs[8] = {x0.x, x0.y, x0.z, x0.w, x1.x, x1.y, x1.z, x1.w};
 #pragma unroll
                 for (int e = 0; e < 4; ++e) {
                     const float2 f = __bfloat1622float2(h[e]);
-                    const int kk = part * (H / 4) + v * 8 + 2 * e;
-                    acc = fmaf(f.x, sh2[kk], acc);
-                    acc = fmaf(f.y, sh2[kk + 1], acc);
+                    acc = fmaf(f.x, xs[2 * e], acc);
+                    acc = fmaf(f.y, xs[2 * e + 1], acc);
                 }
             }
         }
