@@ -788,6 +788,7 @@ static int ivfl2_probes_tc(gn_index *ix, const float *dQ, int64_t nq, int *np_ou
     a.aslot = S.caslot.as<int64_t>();
     a.scores = S.cscores.as<float>();
     a.err = S.err.as<int>();
+    a.next_unit = S.sched.as<unsigned long long>() + 0;
     a.grid = (int)std::min<int64_t>(dev_info().num_sms, units);
     GN_TRY(tc_ivf_launch(a, st));
     const int ncp2 = (int)next_pow2(S.nc);
@@ -825,6 +826,7 @@ int ivfl2_prepare_tc(gn_index *ix, cudaStream_t st) {
     to_bf16_rows(S.cent.as<float>(), S.nc, S.d, S.dp, S.c16.p, S.K, st);
     GN_TRY(S.err.ensure(4));
     GN_CUDA_TRY(cudaMemsetAsync(S.err.p, 0, 4, st));
+    GN_TRY(S.sched.ensure(2 * sizeof(unsigned long long)));
     GN_CUDA_TRY(cudaGetLastError());
     return GN_OK;
 }
@@ -873,6 +875,7 @@ int ivfl2_search_tc(gn_index *ix, const float *dQ, int64_t nq, int k, int64_t *d
     a.aslot = S.aslot.as<int64_t>();
     a.scores = S.scores.as<float>();
     a.err = S.err.as<int>();
+    a.next_unit = S.sched.as<unsigned long long>() + 1;
     a.grid = dev_info().num_sms;
     timing_begin(st, "tc_ivf_kernel");
     GN_TRY(tc_ivf_launch(a, st));

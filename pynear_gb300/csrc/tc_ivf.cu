@@ -4,7 +4,9 @@
 // TMEM lane) and the queries probing the list are the N side, N = 32, 64, 128
 // or 256 (the smallest that holds the work unit's queries), so the MMA work
 // follows the number of queries actually probing the list.  One persistent CTA
-// per SM walks the work units (list, chunk of <= 256 queries, chunk of rows):
+// per SM takes work units (list, chunk of <= 256 queries, chunk of rows) from
+// an atomic counter, largest lists first; warp 0 hands each unit index to the
+// other warps through a 4-slot ring of mbarriers:
 //   warp 0     TMA: per 64-wide K slice, 128 list rows (BF16) and the unit's
 //              N query rows (BF16, bucket order) into a 3-stage ring;
 //   warp 1     TMEM (2 x 256 columns) and tcgen05.mma M=128, N, K=16;
@@ -28,6 +30,7 @@ constexpr int TI_B_BYTES = TI_NMAX * TI_BK * 2;    // 32 KB (max)
 constexpr int TI_STAGE_BYTES = TI_A_BYTES + TI_B_BYTES;
 constexpr int TI_NEPI = 8;
 constexpr int TI_THREADS = 64 + 32 * TI_NEPI;
+constexpr int TI_UR = 4;  // ring of unit indices handed from the producer to the MMA and epilogue warps
 constexpr size_t TI_SMEM = 1024 + (size_t)TI_STAGES * TI_STAGE_BYTES + 256;
 
 __device__ __forceinline__ int ti_nsel(int na) { return na <= 32 ? 32 : na <= 64 ? 64 : na <= 128 ? 128 : 256; }
@@ -37,13 +40,16 @@ __global__ void __launch_bounds__(TI_THREADS, 1)
                   const __grid_constant__ CUtensorMap tmQ64, const __grid_constant__ CUtensorMap tmQ128,
                   const __grid_constant__ CUtensorMap tmQ256, const TcUnit *__restrict__ units,
                   const int64_t *__restrict__ n_units_ptr, int K, const float *__restrict__ xnorm,
-                  const int64_t *__restrict__ aslot, float *__restrict__ scores, int *__restrict__ err) {
+                  const int64_t *__restrict__ aslot, float *__restrict__ scores, int *__restrict__ err,
+                  unsigned long long *__restrict__ next_unit) {
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
     uint64_t *bars = reinterpret_cast<uint64_t *>(smem + TI_STAGES * TI_STAGE_BYTES);
     uint64_t *full = bars, *empty = bars + TI_STAGES, *accfull = bars + 2 * TI_STAGES,
              *accempty = bars + 2 * TI_STAGES + 2;
     uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 2 * TI_STAGES + 4);
+    uint64_t *ufull = bars + 2 * TI_STAGES + 5, *uempty = ufull + TI_UR;
+    volatile int64_t *uring = reinterpret_cast<volatile int64_t *>(uempty + TI_UR);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     volatile int *verr = err;
 
@@ -55,6 +61,10 @@ __global__ void __launch_bounds__(TI_THREADS, 1)
         for (int b = 0; b < 2; ++b) {
             mbar_init(accfull + b, 1);
             mbar_init(accempty + b, TI_NEPI);
+        }
+        for (int r = 0; r < TI_UR; ++r) {
+            mbar_init(ufull + r, 1);
+            mbar_init(uempty + r, 1 + TI_NEPI);
         }
         mbar_fence_init();
     }
@@ -70,7 +80,16 @@ __global__ void __launch_bounds__(TI_THREADS, 1)
         if (lane == 0) {
             uint32_t it = 0;
             bool ok = true;
-            for (int64_t u = blockIdx.x; u < n_units && ok; u += gridDim.x) {
+            // units are taken dynamically (atomic counter): unit costs vary
+            // by orders of magnitude, a static split would leave SMs idle
+            for (uint32_t ui = 0; ok; ++ui) {
+                const int r = ui % TI_UR;
+                if (!mbar_wait(uempty + r, ((ui / TI_UR) & 1) ^ 1, verr)) break;
+                int64_t u = (int64_t)atomicAdd(next_unit, 1ull);
+                if (u >= n_units) u = -1;
+                uring[r] = u;
+                mbar_arrive(ufull + r);
+                if (u < 0) break;
                 const TcUnit un = units[u];
                 const int nsel = ti_nsel(un.na);
                 const CUtensorMap *mq = nsel == 32 ? &tmQ32 : nsel == 64 ? &tmQ64 : nsel == 128 ? &tmQ128 : &tmQ256;
@@ -92,7 +111,12 @@ __global__ void __launch_bounds__(TI_THREADS, 1)
         if (lane == 0) {
             uint32_t it = 0, tile_it = 0;
             bool ok = true;
-            for (int64_t u = blockIdx.x; u < n_units && ok; u += gridDim.x) {
+            for (uint32_t ui = 0; ok; ++ui) {
+                const int r = ui % TI_UR;
+                if (!mbar_wait(ufull + r, (ui / TI_UR) & 1, verr)) break;
+                const int64_t u = uring[r];
+                mbar_arrive(uempty + r);
+                if (u < 0) break;
                 const TcUnit un = units[u];
                 const int nsel = ti_nsel(un.na);
                 const uint32_t idesc = idesc_bf16_f32(TI_M, nsel);
@@ -124,7 +148,13 @@ __global__ void __launch_bounds__(TI_THREADS, 1)
         const int grp = (warp - 2) >> 2;  // column chunks grp, grp + 2, ...
         uint32_t tile_it = 0;
         bool ok = true;
-        for (int64_t u = blockIdx.x; u < n_units && ok; u += gridDim.x) {
+        for (uint32_t ui = 0; ok; ++ui) {
+            const int r = ui % TI_UR;
+            if (!mbar_wait(ufull + r, (ui / TI_UR) & 1, verr)) break;
+            const int64_t u = uring[r];
+            __syncwarp();
+            if (lane == 0) mbar_arrive(uempty + r);
+            if (u < 0) break;
             const TcUnit un = units[u];
             const int nsel = ti_nsel(un.na);
             const int nchunk = nsel / 32;
@@ -216,8 +246,10 @@ int tc_ivf_launch(const TcIvfLaunch &a, cudaStream_t st) {
         GN_CUDA_TRY(cudaFuncSetAttribute(tc_ivf_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TI_SMEM));
         attr = true;
     }
+    if (!a.next_unit) return fail(GN_ERR_INVALID, "tensor-core list scan: no unit counter");
+    GN_CUDA_TRY(cudaMemsetAsync(a.next_unit, 0, sizeof(unsigned long long), st));
     tc_ivf_kernel<<<a.grid, TI_THREADS, TI_SMEM, st>>>(mx, m32, m64, m128, m256, a.units, a.n_units, a.K, a.xnorm,
-                                                        a.aslot, a.scores, a.err);
+                                                        a.aslot, a.scores, a.err, a.next_unit);
     GN_CUDA_TRY(cudaGetLastError());
     return GN_OK;
 }

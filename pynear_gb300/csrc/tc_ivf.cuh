@@ -17,6 +17,7 @@ struct TcIvfLaunch {
     const int64_t *aslot = nullptr; // per query row: segment base of its (query, probe) pair
     float *scores = nullptr;
     int *err = nullptr;
+    unsigned long long *next_unit = nullptr;  // device counter of the dynamic unit schedule (reset per launch)
     int grid = 0;
 };
 
