@@ -328,7 +328,8 @@ def bench_ivf(args, dist, peaks, peak_src):
     _lib.check(lib.gn_ivfl2_last_work(ix._h.h, w.ctypes.data_as(ctypes.c_void_p)))
     pairs, scored, rows, units = (int(x) for x in w)
     kpad = ((IVF_D + 63) // 64) * 64
-    bytes_alg = rows * kpad * 2 + scored * 4          # BF16 list rows read once + FP32 scores written
+    # BF16 list rows read once + FP32 scores written + 16-byte minima per 128-row score slot
+    bytes_alg = rows * kpad * 2 + scored * 4 + (scored // 128 + pairs) * 16
     name_v = name.value.decode()
     flops_alg = 2.0 * IVF_D * scored                 # useful MACs x 2
     kms = t.value

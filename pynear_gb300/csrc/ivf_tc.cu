@@ -172,7 +172,6 @@ __device__ __forceinline__ void block_bitonic_sort(uint64_t *a, int n) {
 }
 
 constexpr int SEL_PCH = 256;   // probes staged per pass
-constexpr int SEL_EPT = 16;    // scores per lane per warp chunk (chunk = 512 scores)
 constexpr int SEL_WB = 512;    // candidate keys buffered per warp
 
 // Ascending bitonic sort of n (power of two, <= 512) keys in shared memory by
@@ -269,69 +268,113 @@ __device__ int block_radix_select(const uint64_t *keys, int WB, const int *cnt, 
     return sh[3];
 }
 
-// Selection of one query by B blocks of 256 threads (B = 1 for large batches;
+// k-th smallest (1-based) of n unsigned values in shared memory, by the whole
+// block (radix select on 8-bit digits); all ones if n < kth.
+template <int NT>
+__device__ uint32_t block_kth_u32(const uint32_t *v, int n, int kth, int *hist, int *sh) {
+    if (n < kth) return 0xffffffffu;
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    uint32_t prefix = 0, mask = 0;
+    int need = kth;
+    for (int shift = 24; shift >= 0; shift -= 8) {
+        for (int i = t; i < 256; i += NT) hist[i] = 0;
+        __syncthreads();
+        for (int i = t; i < n; i += NT) {
+            const uint32_t x = v[i];
+            if ((x & mask) == prefix) atomicAdd(&hist[(x >> shift) & 255], 1);
+        }
+        __syncthreads();
+        if (warp == 0) {
+            int h[8], sum = 0;
+#pragma unroll
+            for (int e = 0; e < 8; ++e) {
+                h[e] = hist[lane * 8 + e];
+                sum += h[e];
+            }
+            int inc = sum;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int x = __shfl_up_sync(0xffffffffu, inc, o);
+                if (lane >= o) inc += x;
+            }
+            int before = inc - sum;
+#pragma unroll
+            for (int e = 0; e < 8; ++e) {
+                if (before < need && need <= before + h[e]) {
+                    sh[0] = lane * 8 + e;
+                    sh[1] = before;
+                }
+                before += h[e];
+            }
+        }
+        __syncthreads();
+        prefix |= (uint32_t)sh[0] << shift;
+        mask |= 0xffu << shift;
+        need -= sh[1];
+        __syncthreads();
+    }
+    return prefix;
+}
+
+// Selection of one query by B blocks of NT threads (B = 1 for large batches;
 // small batches split each query's range over up to 16 blocks, whose partial
-// best-S lists the last block to finish merges).  The query's score segments
-// (one per probed list, in probe order) form one flat range, swept in chunks
-// of 512 scores, chunk c by warp c mod 8, 16 coalesced loads per lane in
-// flight.  Keys are (score, row), so ties go to the lower row.
-//   threshold  from the block's first 8 chunks: a 256-bin histogram of their
-//              ordered score bits over [min, max]; the upper edge of the bin
-//              holding their S-th smallest is an upper bound of the query's
-//              S-th best score;
-//   filter     a score passes if it is not above the thresholds, so almost
-//              every chunk is rejected by one compare per score and one vote
-//              per warp;
-//   buffer     passing keys go to the warp's own shared-memory buffer (512
-//              keys); a full buffer is sorted and cut to its best S, which
-//              lowers the warp's threshold and the block's;
+// best-S lists the last block to finish merges).  The list scan leaves, per
+// (query, list) pair, the scores of the list's rows in 128-row slots and the
+// minimum score of every 32-row quarter of every slot.  Keys are (score, row),
+// so ties go to the lower row.
+//   threshold  tau = the S-th smallest slot minimum of the block's slots
+//              (radix select): S distinct rows score <= tau, so tau bounds the
+//              query's S-th best score;
+//   sweep      warps take 8 slots at a time (lane l: quarter l % 4 of slot
+//              l / 4) and load only the 32-row quarters whose minimum is
+//              <= tau (one coalesced 128-byte load each, four in flight) —
+//              typically a few dozen of the query's hundreds of slots;
+//   buffer     scores <= tau become keys in the warp's shared-memory buffer
+//              (512 keys); a full buffer is sorted and cut to its best S;
 //   select     radix select of the S smallest keys of all warps' buffers;
-//   re-rank    warp per candidate: exact squared L2 in FP32 (compensated sum);
-//              warp 0 returns the k nearest, ties to the lower original index.
-// No block barrier runs inside the sweep.
+//   re-rank    two rows per warp at a time: exact squared L2 in FP32
+//              (compensated sum); warp 0 returns the k nearest, ties to the
+//              lower original index.
 template <int NT>
 __global__ void __launch_bounds__(NT, 1024 / NT) ivf_tc_select_kernel(
-    const float *__restrict__ scores, const int32_t *__restrict__ probes, int np, const int64_t *__restrict__ qseg,
-    const int64_t *__restrict__ seg_rel, const int64_t *__restrict__ list_off, int S, const float *__restrict__ Q,
-    const float *__restrict__ X, int d, int dp, const int32_t *__restrict__ ids, int64_t nq, int k, int B,
-    uint64_t *__restrict__ part, int *__restrict__ done, int64_t *__restrict__ out_idx, float *__restrict__ out_dist,
-    int64_t *__restrict__ out_cnt) {
+    const float *__restrict__ scores, const uint4 *__restrict__ tmin4, const int32_t *__restrict__ probes, int np,
+    const int64_t *__restrict__ qseg, const int64_t *__restrict__ seg_rel, const int64_t *__restrict__ list_off,
+    int S, const float *__restrict__ Q, const float *__restrict__ X, int d, int dp, const int32_t *__restrict__ ids,
+    int64_t nq, int k, int B, uint64_t *__restrict__ part, int *__restrict__ done, int64_t *__restrict__ out_idx,
+    float *__restrict__ out_dist, int64_t *__restrict__ out_cnt) {
     constexpr int NW = NT / 32;
-    constexpr int CH = 32 * SEL_EPT;
     __shared__ uint64_t wreg[NW * SEL_WB];
-    __shared__ int64_t p_seg[SEL_PCH], p_lb[SEL_PCH], p_pre[SEL_PCH + 1];
+    __shared__ int64_t p_slot[SEL_PCH], p_lb[SEL_PCH], p_len[SEL_PCH], p_tpre[SEL_PCH + 1];
     __shared__ int64_t w_sum[NW];
     __shared__ uint64_t sel[64], s_rk[64];
     __shared__ int hist[256], sh[4], s_wn[NW];
-    __shared__ unsigned long long s_thr;
-    __shared__ unsigned int s_u[2];
-    __shared__ int s_nv, s_last;
+    __shared__ int s_last;
     const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
     const int64_t q = blockIdx.x / B;
-    const int bq = (int)(blockIdx.x % B);  // this block's share of the query's range (B > 1 needs np <= SEL_PCH)
+    const int bq = (int)(blockIdx.x % B);  // this block's share of the query's slots (B > 1 needs np <= SEL_PCH)
     uint64_t *W = wreg + warp * SEL_WB;
-    if (t == 0) s_thr = KEY_EMPTY;
-    __syncthreads();
     int wn = 0;                 // keys in this warp's buffer (warp-uniform)
-    uint64_t wthr = KEY_EMPTY;  // this warp's threshold
+    uint64_t wthr = KEY_EMPTY;  // this warp's threshold (its S-th best key after a cut)
+    uint32_t tau = 0xffffffffu;
 
     for (int p0 = 0; p0 < np; p0 += SEL_PCH) {
         const int pc = min(SEL_PCH, np - p0);
-        // per-probe metadata and the prefix sum of the segment lengths
-        int64_t len = 0;
+        // per-probe metadata and the prefix sum of the slot counts
+        int64_t nslot = 0;
         if (t < pc) {
             const int64_t pair = q * np + p0 + t;
             const int32_t l = probes[pair];
+            p_lb[t] = 0;
+            p_len[t] = 0;
+            p_slot[t] = 0;
             if (l >= 0) {
                 p_lb[t] = list_off[l];
-                len = list_off[l + 1] - p_lb[t];
-                p_seg[t] = qseg[q] + seg_rel[pair];
-            } else {
-                p_lb[t] = 0;
-                p_seg[t] = 0;
+                p_len[t] = list_off[l + 1] - p_lb[t];
+                p_slot[t] = qseg[q] + seg_rel[pair];
+                nslot = (p_len[t] + 127) >> 7;
             }
         }
-        int64_t inc = len;
+        int64_t inc = nslot;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
             const int64_t v = __shfl_up_sync(0xffffffffu, inc, o);
@@ -341,155 +384,89 @@ __global__ void __launch_bounds__(NT, 1024 / NT) ivf_tc_select_kernel(
         __syncthreads();
         int64_t before = 0;
         for (int w = 0; w < warp; ++w) before += w_sum[w];
-        if (t < pc) p_pre[t + 1] = before + inc;
-        if (t == 0) p_pre[0] = 0;
+        if (t < pc) p_tpre[t + 1] = before + inc;
+        if (t == 0) p_tpre[0] = 0;
         __syncthreads();
-        const int64_t all = p_pre[pc];
-        const int64_t lo = all * bq / B, hi = all * (bq + 1) / B;
-        int pw = 0;  // probe of the chunk start (monotone over the warp's chunks)
-        uint32_t v[SEL_EPT];  // ordered score bits (f2ord)
-        uint32_t valid = 0;
-        bool full = false;
-        // chunk [c0, min(c0 + 512, hi)) into v[] (lane l: scores c0 + 32 j + l)
-        auto load = [&](int64_t c0) {
-            const int64_t cend = min(c0 + CH, hi);
-            while (p_pre[pw + 1] <= c0) ++pw;
-            const bool one = cend <= p_pre[pw + 1];  // chunk inside one segment
-            full = cend - c0 == CH;
-            if (one && full) {
-                const float *src = scores + p_seg[pw] + (c0 - p_pre[pw]) + lane;
-#pragma unroll
-                for (int j = 0; j < SEL_EPT; ++j) v[j] = f2ord(__ldg(src + j * 32));
-                valid = 0xffffu;
-            } else {
-                valid = 0;
-#pragma unroll
-                for (int j = 0; j < SEL_EPT; ++j) {
-                    const int64_t f = c0 + j * 32 + lane;
-                    v[j] = 0xffffffffu;
-                    if (f < cend) {
-                        int p = pw;
-                        while (p_pre[p + 1] <= f) ++p;
-                        v[j] = f2ord(__ldg(scores + p_seg[p] + (f - p_pre[p])));
-                        valid |= 1u << j;
-                    }
-                }
-            }
-        };
-        int64_t c0 = lo + (int64_t)warp * CH;
-        if (c0 < hi) load(c0);
+        const int64_t all = p_tpre[pc];
+        // parts actually used: at least 2S slots each, so that every part's
+        // threshold comes from enough slot minima (idle parts publish nothing)
+        const int bu = (int)max((int64_t)1, min((int64_t)B, all / (2 * S)));
+        const int64_t lo = bq < bu ? all * bq / bu : all, hi = bq < bu ? all * (bq + 1) / bu : all;
         if (p0 == 0) {
-            // block threshold from the block's first 8 chunks: an upper
-            // bound of their S-th smallest score, hence of the query's
-            uint32_t mn = 0xffffffffu, mx = 0;
-#pragma unroll
-            for (int j = 0; j < SEL_EPT; ++j) {
-                if ((valid >> j) & 1u) {
-                    mn = min(mn, v[j]);
-                    mx = max(mx, v[j]);
-                }
-            }
-            mn = __reduce_min_sync(0xffffffffu, mn);
-            mx = __reduce_max_sync(0xffffffffu, mx);
-            const int nv = __reduce_add_sync(0xffffffffu, __popc(valid));
-            if (t == 0) {
-                s_u[0] = 0xffffffffu;
-                s_u[1] = 0;
-                s_nv = 0;
-            }
-            for (int i = t; i < 256; i += NT) hist[i] = 0;
-            __syncthreads();
-            if (lane == 0) {
-                atomicMin(&s_u[0], mn);
-                atomicMax(&s_u[1], mx);
-                atomicAdd(&s_nv, nv);
+            // threshold from the block's first slots (any S of them bound it)
+            uint32_t *tm = reinterpret_cast<uint32_t *>(wreg);
+            const int na = (int)min(hi - lo, (int64_t)NW * SEL_WB * 2);
+            int p = 0;
+            for (int i = t; i < na; i += NT) {
+                const int64_t f = lo + i;
+                while (p_tpre[p + 1] <= f) ++p;
+                const uint4 m = __ldg(tmin4 + p_slot[p] + (f - p_tpre[p]));
+                tm[i] = min(min(m.x, m.y), min(m.z, m.w));
             }
             __syncthreads();
-            if (s_nv >= S) {
-                // 256-bin histogram of the sample over [min, max]; the upper
-                // edge of the bin holding the S-th smallest bounds it
-                const uint32_t lo_o = s_u[0], range = s_u[1] - lo_o;
-                const int sh_b = max(0, 24 - __clz(range | 1));  // (range >> sh_b) < 256
-#pragma unroll
-                for (int j = 0; j < SEL_EPT; ++j)
-                    if ((valid >> j) & 1u) atomicAdd(&hist[(v[j] - lo_o) >> sh_b], 1);
-                __syncthreads();
-                if (warp == 0) {
-                    int h[8], sum = 0;
-#pragma unroll
-                    for (int e = 0; e < 8; ++e) {
-                        h[e] = hist[lane * 8 + e];
-                        sum += h[e];
-                    }
-                    int inc = sum;
-#pragma unroll
-                    for (int o = 1; o < 32; o <<= 1) {
-                        const int x = __shfl_up_sync(0xffffffffu, inc, o);
-                        if (lane >= o) inc += x;
-                    }
-                    int before = inc - sum;
-#pragma unroll
-                    for (int e = 0; e < 8; ++e) {
-                        if (before < S && S <= before + h[e]) {
-                            const uint64_t edge = (uint64_t)lo_o + ((uint64_t)(lane * 8 + e + 1) << sh_b) - 1;
-                            s_thr = make_key((uint32_t)min(edge, (uint64_t)s_u[1]), 0xffffffffu);
-                        }
-                        before += h[e];
-                    }
-                }
-            }
-            __syncthreads();
-            wthr = s_thr;
+            tau = block_kth_u32<NT>(tm, na, S, hist, sh);
+            wthr = tau == 0xffffffffu ? KEY_EMPTY : make_key(tau, 0xffffffffu);
         }
-        while (c0 < hi) {
-            uint64_t thr = min(wthr, (uint64_t)*reinterpret_cast<volatile unsigned long long *>(&s_thr));
-            const uint32_t thr_o = key_dist(thr);
-            uint32_t pend = 0;
+        int p = 0;  // probe of this lane's slot (monotone over the sweep)
+        // warp w takes 8 slots at a time: lane l looks at quarter l % 4 of slot g0 + l / 4
+        for (int64_t g0 = lo + (int64_t)warp * 8; g0 < hi; g0 += (int64_t)NW * 8) {
+            const int64_t f = g0 + (lane >> 2);
+            const int qu = lane & 3;
+            bool qual = false;
+            if (f < hi) {
+                while (p_tpre[p + 1] <= f) ++p;
+                qual = __ldg(reinterpret_cast<const uint32_t *>(tmin4 + p_slot[p] + (f - p_tpre[p])) + qu) <= tau;
+            }
+            unsigned bal = __ballot_sync(0xffffffffu, qual);
+            while (bal) {
+                // up to four qualifying quarters at a time, their loads in flight together
+                int src[4], nb = 0;
 #pragma unroll
-            for (int j = 0; j < SEL_EPT; ++j) pend |= (v[j] <= thr_o ? 1u : 0u) << j;
-            pend &= valid;
-            uint32_t wpend = __reduce_or_sync(0xffffffffu, pend);  // positions pending in some lane
-            while (wpend) {
-                // one position at a time (warp-uniform); the body is not
-                // unrolled, to keep the kernel small for the instruction cache
-                for (uint32_t bits = wpend; bits; bits &= bits - 1) {
-                    const int j = __ffs(bits) - 1;
-                    uint32_t vj = 0;
-#pragma unroll
-                    for (int jj = 0; jj < SEL_EPT; ++jj) vj = jj == j ? v[jj] : vj;
-                    bool want = (pend >> j) & 1u;
-                    uint64_t key = KEY_EMPTY;
-                    if (want) {
-                        const int64_t f = c0 + j * 32 + lane;
-                        int p = pw;
-                        while (p_pre[p + 1] <= f) ++p;
-                        key = make_key(vj, (uint32_t)(p_lb[p] + (f - p_pre[p])));
-                        want = key < thr;
-                        if (!want) pend &= ~(1u << j);
-                    }
-                    const unsigned bal = __ballot_sync(0xffffffffu, want);
+                for (int u = 0; u < 4; ++u) {
+                    src[u] = bal ? __ffs(bal) - 1 : -1;
                     if (bal) {
-                        const int pos = wn + __popc(bal & ((1u << lane) - 1u));
-                        if (want && pos < SEL_WB) {
-                            W[pos] = key;
-                            pend &= ~(1u << j);
-                        }
-                        wn += __popc(bal);
+                        bal &= bal - 1;
+                        ++nb;
                     }
                 }
-                if (wn <= SEL_WB) break;
-                // full: keep the best S, keys that did not fit are offered again
-                __syncwarp();
-                warp_bitonic_sort(W, SEL_WB, lane);
-                wthr = W[S - 1];
-                if (lane == 0) atomicMin(&s_thr, (unsigned long long)wthr);
-                wn = S;
-                thr = min(wthr, (uint64_t)*reinterpret_cast<volatile unsigned long long *>(&s_thr));
-                wpend = __reduce_or_sync(0xffffffffu, pend);
-                __syncwarp();
+                uint32_t v[4];
+                uint64_t key[4];
+                bool want[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const int sl = src[u] < 0 ? 0 : src[u];
+                    const int pp = __shfl_sync(0xffffffffu, p, sl);
+                    const int64_t slot = g0 + (sl >> 2) - p_tpre[pp];
+                    const int i = (sl & 3) * 32 + lane;  // row within the slot
+                    const int64_t r0 = slot * 128;
+                    const bool ok = u < nb && r0 + i < p_len[pp];
+                    v[u] = ok ? f2ord(__ldg(scores + (p_slot[pp] + slot) * 128 + i)) : 0xffffffffu;
+                    key[u] = make_key(v[u], (uint32_t)(p_lb[pp] + r0 + i));
+                    want[u] = ok;
+                }
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    bool w = want[u] && key[u] < wthr;
+                    while (true) {
+                        const unsigned b2 = __ballot_sync(0xffffffffu, w);
+                        if (!b2) break;
+                        const int pos = wn + __popc(b2 & ((1u << lane) - 1u));
+                        if (w && pos < SEL_WB) {
+                            W[pos] = key[u];
+                            w = false;
+                        }
+                        wn += __popc(b2);
+                        if (wn <= SEL_WB) break;
+                        // full: keep the best S; keys that did not fit are offered again
+                        __syncwarp();
+                        warp_bitonic_sort(W, SEL_WB, lane);
+                        wthr = W[S - 1];
+                        wn = S;
+                        w = w && key[u] < wthr;
+                        __syncwarp();
+                    }
+                }
             }
-            c0 += (int64_t)NW * CH;
-            if (c0 < hi) load(c0);
         }
         __syncthreads();
     }
@@ -844,7 +821,9 @@ int ivfl2_search_tc(gn_index *ix, const float *dQ, int64_t nq, int k, int64_t *d
     // work items of rc rows (short items for small batches so that their few
     // lists still spread over all SMs); every pair owns a score segment
     const int rc = nq >= 512 ? S.rc_tc : (nq >= 64 ? 1024 : 256);
-    GN_TRY(ivf_plan(T, nq, np, S.nc, S.list_off.as<int64_t>(), rc, TC_QCHUNK, st, 1));
+    // score segments in 128-row slots: slot_rel / qslot count slots, and a
+    // pair's tile t has its minima at tmin4[(slot base + t) * 4 ...]
+    GN_TRY(ivf_plan(T, nq, np, S.nc, S.list_off.as<int64_t>(), rc, TC_QCHUNK, st, 128));
     const int64_t npairs = nq * np;
     const int64_t qb_rows = std::max<int64_t>(npairs, 256);  // >= one 256-row TMA box
     GN_TRY(S.qb.ensure((size_t)qb_rows * S.K * 2));
@@ -861,8 +840,12 @@ int ivfl2_search_tc(gn_index *ix, const float *dQ, int64_t nq, int k, int64_t *d
         T.item_off.as<int64_t>(), S.nc, T.boff.as<int64_t>(), S.list_off.as<int64_t>(), rc, max_units,
         S.units.as<TcUnit>(), S.nunits.as<int64_t>());
     // score segments: at most the rows of the np largest lists per query
-    const int64_t seg_total = nq * S.top_rows[(size_t)std::min<int64_t>(np, (int64_t)S.top_rows.size() - 1)];
-    GN_TRY(S.scores.ensure((size_t)std::max<int64_t>(seg_total, 1) * 4));
+    // score slots: at most the rows of the np largest lists per query, plus one
+    // partial slot per probe
+    const int64_t np_eff = std::min<int64_t>(np, (int64_t)S.top_rows.size() - 1);
+    const int64_t slots_total = nq * (ceil_div(S.top_rows[(size_t)np_eff], 128) + np);
+    GN_TRY(S.scores.ensure((size_t)std::max<int64_t>(slots_total, 1) * 128 * 4));
+    GN_TRY(S.tmin.ensure((size_t)std::max<int64_t>(slots_total, 1) * 4 * 4));
     TcIvfLaunch a;
     a.X = S.x16.p;
     a.x_rows = std::max<int64_t>(S.n, 256);
@@ -873,7 +856,9 @@ int ivfl2_search_tc(gn_index *ix, const float *dQ, int64_t nq, int k, int64_t *d
     a.n_units = S.nunits.as<int64_t>();
     a.xnorm = S.vnorm.as<float>();
     a.aslot = S.aslot.as<int64_t>();
+    a.seg_mul = 128;
     a.scores = S.scores.as<float>();
+    a.tmin4 = S.tmin.as<uint32_t>();
     a.err = S.err.as<int>();
     a.next_unit = S.sched.as<unsigned long long>() + 1;
     a.grid = dev_info().num_sms;
@@ -903,7 +888,8 @@ int ivfl2_search_tc(gn_index *ix, const float *dQ, int64_t nq, int k, int64_t *d
             carve = true;
         }
         ivf_tc_select_kernel<NT><<<blocks, NT, 0, st>>>(
-            S.scores.as<float>(), T.probes.as<int32_t>(), np, T.qslot.as<int64_t>(), T.slot_rel.as<int64_t>(),
+            S.scores.as<float>(), S.tmin.as<uint4>(), T.probes.as<int32_t>(), np, T.qslot.as<int64_t>(),
+            T.slot_rel.as<int64_t>(),
             S.list_off.as<int64_t>(), S.shortlist, dQ, S.vecs.as<float>(), S.d, S.dp, S.ids.as<int32_t>(), nq, k, B,
             S.sel_part.as<uint64_t>(), S.sel_done.as<int>(), d_idx, d_dist, d_cnt);
         return GN_OK;

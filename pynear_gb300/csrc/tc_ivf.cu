@@ -13,7 +13,9 @@
 //   warps 2-9  epilogue: thread = list row; for each query column its score
 //              |x|^2 - 2 q.x (exact FP32 |x|^2) goes to that (query, probe)
 //              pair's segment at the row's offset — 32 lanes write 32
-//              consecutive rows, so every store is one 128-byte line.
+//              consecutive rows, so every store is one 128-byte line — and,
+//              for the list scan, the minimum score of each 32-row quarter
+//              of the 128-row tile goes to the pair's tile-minimum array.
 #include <cuda_bf16.h>
 
 #include <algorithm>
@@ -33,6 +35,12 @@ constexpr int TI_THREADS = 64 + 32 * TI_NEPI;
 constexpr int TI_UR = 4;  // ring of unit indices handed from the producer to the MMA and epilogue warps
 constexpr size_t TI_SMEM = 1024 + (size_t)TI_STAGES * TI_STAGE_BYTES + 256;
 
+// order-preserving map of a float to an unsigned key
+__device__ __forceinline__ uint32_t ti_ord(float f) {
+    const uint32_t u = __float_as_uint(f);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+
 __device__ __forceinline__ int ti_nsel(int na) { return na <= 32 ? 32 : na <= 64 ? 64 : na <= 128 ? 128 : 256; }
 
 __global__ void __launch_bounds__(TI_THREADS, 1)
@@ -40,8 +48,8 @@ __global__ void __launch_bounds__(TI_THREADS, 1)
                   const __grid_constant__ CUtensorMap tmQ64, const __grid_constant__ CUtensorMap tmQ128,
                   const __grid_constant__ CUtensorMap tmQ256, const TcUnit *__restrict__ units,
                   const int64_t *__restrict__ n_units_ptr, int K, const float *__restrict__ xnorm,
-                  const int64_t *__restrict__ aslot, float *__restrict__ scores, int *__restrict__ err,
-                  unsigned long long *__restrict__ next_unit) {
+                  const int64_t *__restrict__ aslot, int seg_mul, float *__restrict__ scores,
+                  uint32_t *__restrict__ tmin4, int *__restrict__ err, unsigned long long *__restrict__ next_unit) {
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
     uint64_t *bars = reinterpret_cast<uint64_t *>(smem + TI_STAGES * TI_STAGE_BYTES);
@@ -158,12 +166,12 @@ __global__ void __launch_bounds__(TI_THREADS, 1)
             const TcUnit un = units[u];
             const int nsel = ti_nsel(un.na);
             const int nchunk = nsel / 32;
-            // segment base (minus the list start) of query column c*32 + lane
+            // segment base (aslot x seg_mul, minus the list start) of query column c*32 + lane
             int64_t segv[TI_NMAX / 32 / 2];
 #pragma unroll
             for (int cc = 0; cc < TI_NMAX / 32 / 2; ++cc) {
                 const int col = (grp + 2 * cc) * 32 + lane;
-                segv[cc] = (col < un.na) ? aslot[un.a0 + col] - un.rbase : INT64_MIN;
+                segv[cc] = (col < un.na) ? aslot[un.a0 + col] * seg_mul - un.rbase : INT64_MIN;
             }
             const int ntile = (int)((un.r1 - un.r0 + TI_M - 1) / TI_M);
             for (int t = 0; t < ntile; ++t, ++tile_it) {
@@ -183,10 +191,22 @@ __global__ void __launch_bounds__(TI_THREADS, 1)
 #pragma unroll
                     for (int z = 1; z < TI_NMAX / 32 / 2; ++z)
                         if (cc == z) sv = segv[z];
+                    uint32_t mymin = 0xffffffffu;  // lane j: this warp's 32-row minimum of column j
 #pragma unroll
                     for (int j = 0; j < 32; ++j) {
                         const int64_t seg = __shfl_sync(0xffffffffu, sv, j);
-                        if (seg != INT64_MIN && rok) scores[seg + row] = fmaf(-2.f, acc[j], xn);
+                        const float v = fmaf(-2.f, acc[j], xn);
+                        if (seg != INT64_MIN && rok) scores[seg + row] = v;
+                        if (tmin4) {
+                            const uint32_t m = __reduce_min_sync(0xffffffffu, rok ? ti_ord(v) : 0xffffffffu);
+                            mymin = lane == j ? m : mymin;
+                        }
+                    }
+                    // tile minimum, one word per 32-row quarter: slot = segment base / 128
+                    // + the tile's index in the list (segments are 128-aligned)
+                    if (tmin4 && sv != INT64_MIN) {
+                        const int64_t tile = (sv + un.rbase) / TI_M + (un.r0 - un.rbase) / TI_M + t;
+                        tmin4[tile * 4 + quad] = mymin;
                     }
                 }
                 tc_fence_before();
@@ -249,7 +269,7 @@ int tc_ivf_launch(const TcIvfLaunch &a, cudaStream_t st) {
     if (!a.next_unit) return fail(GN_ERR_INVALID, "tensor-core list scan: no unit counter");
     GN_CUDA_TRY(cudaMemsetAsync(a.next_unit, 0, sizeof(unsigned long long), st));
     tc_ivf_kernel<<<a.grid, TI_THREADS, TI_SMEM, st>>>(mx, m32, m64, m128, m256, a.units, a.n_units, a.K, a.xnorm,
-                                                        a.aslot, a.scores, a.err, a.next_unit);
+                                                        a.aslot, a.seg_mul, a.scores, a.tmin4, a.err, a.next_unit);
     GN_CUDA_TRY(cudaGetLastError());
     return GN_OK;
 }

@@ -14,8 +14,10 @@ struct TcIvfLaunch {
     const TcUnit *units = nullptr;  // a0/na: query rows, r0/r1: list rows, rbase: list start
     const int64_t *n_units = nullptr;
     const float *xnorm = nullptr;   // |x|^2 of the list rows
-    const int64_t *aslot = nullptr; // per query row: segment base of its (query, probe) pair
+    const int64_t *aslot = nullptr; // per query row: segment base of its (query, probe) pair, in seg_mul units
+    int seg_mul = 1;                // 128 for the list scan: segments are 128-row slots
     float *scores = nullptr;
+    uint32_t *tmin4 = nullptr;      // optional: per (slot, 32-row quarter) minimum ordered score
     int *err = nullptr;
     unsigned long long *next_unit = nullptr;  // device counter of the dynamic unit schedule (reset per launch)
     int grid = 0;

@@ -67,3 +67,25 @@ def test_ivf_tc_engine_matches_exact_within_probed_lists(gn, oracle):
     ix.set_engine("fp32")
     fi, fd, fc = ix.search_knn_arrays(q, 10)
     assert np.mean(fi == idx) >= 0.995
+
+
+def test_ivf_tc_engine_same_results_for_every_batch_split(gn):
+    """Small batches split each query's selection over several blocks; the
+    results must equal those of a large batch (one block per query), with no
+    repeated ids."""
+    rng = np.random.default_rng(7)
+    c = rng.standard_normal((300, 40), dtype=np.float32)
+    db = (c[rng.integers(0, 300, 30000)] + np.float32(0.4) * rng.standard_normal((30000, 40), dtype=np.float32))
+    q = (c[rng.integers(0, 300, 512)] + np.float32(0.4) * rng.standard_normal((512, 40), dtype=np.float32))
+    for nprobe in (1, 5, 24):
+        ix = gn.IVFFlatL2Index(n_clusters=64, n_probe=nprobe, engine="tc")
+        ix.set(db)
+        ref_i, ref_d, ref_c = ix.search_knn_arrays(q, 8)
+        for row in ref_i:
+            v = row[row >= 0]
+            assert len(set(v.tolist())) == len(v)
+        for n in (1, 3, 16, 33, 64, 128, 200):
+            i, d, cnt = ix.search_knn_arrays(q[:n], 8)
+            np.testing.assert_array_equal(i, ref_i[:n])
+            np.testing.assert_array_equal(d, ref_d[:n])
+            np.testing.assert_array_equal(cnt, ref_c[:n])
