@@ -236,6 +236,95 @@ __global__ void __launch_bounds__(1024) ivf_qscan_kernel(const int64_t *__restri
     if (threadIdx.x == 0) qslot[nq] = tot;
 }
 
+// The whole plan of a small batch in one block (replaces the count, plan,
+// fill, slots and scan kernels and their memsets): bucket counts in shared
+// memory, list offsets and work items, bucket fill, per-query slots and their
+// scan.  Same outputs as the multi-kernel plan.
+__global__ void __launch_bounds__(1024) ivf_plan_small_kernel(
+    const int32_t *__restrict__ probes, int64_t nq, int np, int nc, const int64_t *__restrict__ list_off, int rc,
+    int qchunk, int slot_rc, int32_t *__restrict__ bcnt, int64_t *__restrict__ boff, int64_t *__restrict__ item_off,
+    int64_t *__restrict__ bucket, int64_t *__restrict__ slot_rel, int64_t *__restrict__ qcount,
+    int64_t *__restrict__ qslot, int64_t *__restrict__ counter) {
+    extern __shared__ int32_t plan_sm[];  // [nc] counts, [nc] fill cursors
+    int32_t *s_cnt = plan_sm, *s_fill = plan_sm + nc;
+    const int t = threadIdx.x, nt = blockDim.x;
+    const int64_t npairs = nq * np;
+    for (int l = t; l < nc; l += nt) s_cnt[l] = s_fill[l] = 0;
+    if (t == 0) *counter = 0;
+    __syncthreads();
+    for (int64_t i = t; i < npairs; i += nt) {
+        const int32_t l = probes[i];
+        if (l >= 0) atomicAdd(&s_cnt[l], 1);
+    }
+    __syncthreads();
+    {
+        const int per = (nc + nt - 1) / nt;
+        const int b = t * per, e = min(nc, b + per);
+        int64_t sb = 0, si = 0;
+        for (int l = b; l < e; ++l) {
+            const int64_t cnt = s_cnt[l], len = list_off[l + 1] - list_off[l];
+            sb += cnt;
+            si += (cnt > 0 && len > 0) ? ((cnt + qchunk - 1) / qchunk) * ((len + rc - 1) / rc) : 0;
+        }
+        int64_t tb = 0, ti = 0;
+        int64_t xb = block_exclusive_scan(sb, &tb);
+        int64_t xi = block_exclusive_scan(si, &ti);
+        for (int l = b; l < e; ++l) {
+            const int64_t cnt = s_cnt[l], len = list_off[l + 1] - list_off[l];
+            bcnt[l] = (int32_t)cnt;
+            boff[l] = xb;
+            item_off[l] = xi;
+            xb += cnt;
+            xi += (cnt > 0 && len > 0) ? ((cnt + qchunk - 1) / qchunk) * ((len + rc - 1) / rc) : 0;
+        }
+        if (t == 0) {
+            boff[nc] = tb;
+            item_off[nc] = ti;
+        }
+    }
+    __syncthreads();
+    for (int64_t i = t; i < npairs; i += nt) {
+        const int32_t l = probes[i];
+        if (l >= 0) bucket[boff[l] + atomicAdd(&s_fill[l], 1)] = i;
+    }
+    // slots: warp per query
+    const int lane = t & 31;
+    for (int64_t q = t >> 5; q < nq; q += nt >> 5) {
+        int64_t s = 0;
+        for (int p0 = 0; p0 < np; p0 += 32) {
+            const int p = p0 + lane;
+            int64_t c = 0;
+            if (p < np) {
+                const int32_t l = probes[q * np + p];
+                if (l >= 0) c = (list_off[l + 1] - list_off[l] + slot_rc - 1) / slot_rc;
+            }
+            int64_t inc = c;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int64_t v = __shfl_up_sync(0xffffffffu, inc, o);
+                if (lane >= o) inc += v;
+            }
+            if (p < np) slot_rel[q * np + p] = s + inc - c;
+            s += __shfl_sync(0xffffffffu, inc, 31);
+        }
+        if (lane == 0) qcount[q] = s;
+    }
+    __syncthreads();
+    {
+        const int64_t per = (nq + nt - 1) / nt;
+        const int64_t b = t * per, e = min(nq, b + per);
+        int64_t s = 0;
+        for (int64_t i = b; i < e; ++i) s += qcount[i];
+        int64_t tot = 0;
+        int64_t x = block_exclusive_scan(s, &tot);
+        for (int64_t i = b; i < e; ++i) {
+            qslot[i] = x;
+            x += qcount[i];
+        }
+        if (t == 0) qslot[nq] = tot;
+    }
+}
+
 __device__ __forceinline__ int find_list(const int64_t *item_off, int nc, int64_t item) {
     int lo = 0, hi = nc;  // item_off[lo] <= item < item_off[hi]
     while (hi - lo > 1) {
@@ -501,6 +590,9 @@ static int64_t max_slots_per_query(const std::vector<int64_t> &top, int np, int 
     return p + (top[(size_t)p] + rc - 1) / rc;
 }
 
+constexpr int64_t PLAN_SMALL_PAIRS = 16384;  // batches planned by one block
+constexpr int PLAN_SMALL_LISTS = 8192;
+
 // Bucket the (query, probe) pairs by list and plan the work items; probes
 // (int32, nq*np) must be filled.  Produces boff, bucket, item_off, slot_rel,
 // qslot in S.  All on the device, no host synchronisation.
@@ -517,6 +609,22 @@ int ivf_plan(IvfScratch &S, int64_t nq, int np, int nc, const int64_t *d_list_of
     GN_TRY(S.qcount.ensure((size_t)nq * 8));
     GN_TRY(S.qslot.ensure((size_t)(nq + 1) * 8));
     GN_TRY(S.counter.ensure(8));
+    if (npairs <= PLAN_SMALL_PAIRS && nc <= PLAN_SMALL_LISTS) {  // one block does it all
+        const size_t smem = (size_t)nc * 2 * sizeof(int32_t);
+        static bool attr = false;
+        if (!attr) {
+            GN_CUDA_TRY(cudaFuncSetAttribute(ivf_plan_small_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)(PLAN_SMALL_LISTS * 2 * sizeof(int32_t))));
+            attr = true;
+        }
+        ivf_plan_small_kernel<<<1, 1024, smem, st>>>(S.probes.as<int32_t>(), nq, np, nc, d_list_off, rc, qchunk,
+                                                     slot_rc, S.bcnt.as<int32_t>(), S.boff.as<int64_t>(),
+                                                     S.item_off.as<int64_t>(), S.bucket.as<int64_t>(),
+                                                     S.slot_rel.as<int64_t>(), S.qcount.as<int64_t>(),
+                                                     S.qslot.as<int64_t>(), S.counter.as<int64_t>());
+        GN_CUDA_TRY(cudaGetLastError());
+        return GN_OK;
+    }
     GN_CUDA_TRY(cudaMemsetAsync(S.bcnt.p, 0, (size_t)nc * 4, st));
     GN_CUDA_TRY(cudaMemsetAsync(S.fill.p, 0, (size_t)nc * 4, st));
     GN_CUDA_TRY(cudaMemsetAsync(S.counter.p, 0, 8, st));
