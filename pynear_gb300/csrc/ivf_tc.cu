@@ -600,7 +600,7 @@ __global__ void __launch_bounds__(256) coarse_probe_kernel(const float *__restri
             const float4 *cr = reinterpret_cast<const float4 *>(C + (int64_t)c * dp);
             const float4 *qr = reinterpret_cast<const float4 *>(sqr);
             const int n4 = d >> 2;
-#pragma unroll 4
+#pragma unroll 8
             for (int t = part; t < n4; t += 8) {
                 const float4 a = __ldg(cr + t), b = qr[t];
                 float e0 = b.x - a.x, e1 = b.y - a.y, e2 = b.z - a.z, e3 = b.w - a.w;
@@ -622,18 +622,38 @@ __global__ void __launch_bounds__(256) coarse_probe_kernel(const float *__restri
         if (part == 0) sd[i] = s;
     }
     __syncthreads();
-    if (j < NC) skeys[j] = sc[j] >= 0 ? make_key(__float_as_uint(sd[j]), (uint32_t)sc[j]) : KEY_EMPTY;
-    __syncthreads();
-    for (int size = 2; size <= NC; size <<= 1)
-        for (int stride = size >> 1; stride > 0; stride >>= 1) {
-            if (j < NC / 2) {
-                const int lo = 2 * j - (j & (stride - 1)), hi = lo + stride;
-                const bool up = (lo & size) == 0;
-                const uint64_t a = skeys[lo], b = skeys[hi];
-                if ((a > b) == up) { skeys[lo] = b; skeys[hi] = a; }
-            }
-            __syncthreads();
+    if (warp == 0) {
+        // sort the 64 (exact distance, centroid) keys in registers: lane l
+        // holds positions l and l + 32 (bitonic network, shuffles only)
+        uint64_t r2[2];
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int i = h * 32 + lane;
+            r2[h] = sc[i] >= 0 ? make_key(__float_as_uint(sd[i]), (uint32_t)sc[i]) : KEY_EMPTY;
         }
+#pragma unroll
+        for (int size = 2; size <= NC; size <<= 1)
+#pragma unroll
+            for (int stride = size >> 1; stride > 0; stride >>= 1) {
+                if (stride == 32) {
+                    const uint64_t a = r2[0], b = r2[1];
+                    r2[0] = a < b ? a : b;
+                    r2[1] = a < b ? b : a;
+                } else {
+#pragma unroll
+                    for (int h = 0; h < 2; ++h) {
+                        const int i = h * 32 + lane;
+                        const uint64_t y = __shfl_xor_sync(0xffffffffu, r2[h], stride);
+                        const bool lower = (i & stride) == 0, asc = (i & size) == 0;
+                        const bool take_min = lower == asc;
+                        r2[h] = take_min ? (r2[h] < y ? r2[h] : y) : (r2[h] < y ? y : r2[h]);
+                    }
+                }
+            }
+        skeys[lane] = r2[0];
+        skeys[lane + 32] = r2[1];
+    }
+    __syncthreads();
     if (j < NC) {
         const uint64_t k = skeys[j];
         const bool e = k == KEY_EMPTY;
