@@ -34,7 +34,7 @@
 
 namespace gn {
 
-constexpr int TC_QCHUNK = 256;  // queries per tensor-core work unit (MMA N <= 256)
+constexpr int TC_QCHUNK = 128;  // queries per tensor-core work unit (MMA N <= 128)
 
 // Qb row pos = BF16 row of the query of the pair bucket[pos]; warp per row.
 __global__ void qb_fill_kernel(const uint4 *__restrict__ q16, int K8, int np, const int64_t *__restrict__ bucket,
@@ -70,8 +70,11 @@ __global__ void tc_units_kernel(const int64_t *__restrict__ item_off, int nc, co
     const int l = find_list_tc(item_off, nc, i);
     const int64_t lb = list_off[l], le = list_off[l + 1];
     const int64_t nrc = (le - lb + rc - 1) / rc;
+    const int64_t nqc = nrc > 0 ? (item_off[l + 1] - item_off[l]) / nrc : 1;
     const int64_t local = i - item_off[l];
-    const int64_t qc = local / nrc, rch = local % nrc;
+    // the query chunks of one row chunk are adjacent: taken together by
+    // different SMs, their second and later reads of the rows hit L2
+    const int64_t rch = local / nqc, qc = local % nqc;
     TcUnit u;
     u.a0 = boff[l] + qc * TC_QCHUNK;
     u.na = (int32_t)min((int64_t)TC_QCHUNK, boff[l + 1] - u.a0);
@@ -543,14 +546,14 @@ __global__ void __launch_bounds__(NT, 1024 / NT) ivf_tc_select_kernel(
 __global__ void coarse_units_kernel(int64_t nq, int nc, TcUnit *__restrict__ units, int64_t *__restrict__ n_units,
                                     int64_t *__restrict__ aslot) {
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const int64_t nqc = (nq + 255) / 256, ncc = (nc + 127) / 128;
+    const int64_t nqc = (nq + TC_QCHUNK - 1) / TC_QCHUNK, ncc = (nc + 127) / 128;
     if (t == 0) *n_units = nqc * ncc;
     if (t < nq) aslot[t] = t * nc;
     if (t >= nqc * ncc) return;
     const int64_t qc = t / ncc, cc = t % ncc;
     TcUnit u;
-    u.a0 = qc * 256;
-    u.na = (int32_t)min((int64_t)256, nq - u.a0);
+    u.a0 = qc * TC_QCHUNK;
+    u.na = (int32_t)min((int64_t)TC_QCHUNK, nq - u.a0);
     u.r0 = cc * 128;
     u.r1 = min((int64_t)nc, u.r0 + 128);
     u.rbase = 0;
@@ -765,7 +768,7 @@ static int ivfl2_probes_tc(gn_index *ix, const float *dQ, int64_t nq, int *np_ou
         return ivfl2_coarse(ix, dQ, nq, *np_out, st);
     }
     *np_out = np;
-    const int64_t units = ceil_div(nq, 256) * ceil_div(S.nc, 128);
+    const int64_t units = ceil_div(nq, TC_QCHUNK) * ceil_div(S.nc, 128);
     GN_TRY(S.cunits.ensure((size_t)units * sizeof(TcUnit)));
     GN_TRY(S.cnunits.ensure(8));
     GN_TRY(S.caslot.ensure((size_t)nq * 8));
@@ -840,7 +843,7 @@ int ivfl2_search_tc(gn_index *ix, const float *dQ, int64_t nq, int k, int64_t *d
     GN_TRY(ivfl2_probes_tc(ix, dQ, nq, &np, st));
     // work items of rc rows (short items for small batches so that their few
     // lists still spread over all SMs); every pair owns a score segment
-    const int rc = nq >= 512 ? S.rc_tc : (nq >= 64 ? 1024 : 256);
+    const int rc = nq >= 64 ? 1024 : 256;
     // score segments in 128-row slots: slot_rel / qslot count slots, and a
     // pair's tile t has its minima at tmin4[(slot base + t) * 4 ...]
     GN_TRY(ivf_plan(T, nq, np, S.nc, S.list_off.as<int64_t>(), rc, TC_QCHUNK, st, 128));

@@ -26,9 +26,9 @@
 
 namespace gn {
 
-constexpr int TI_M = 128, TI_NMAX = 256, TI_BK = 64, TI_STAGES = 3;
+constexpr int TI_M = 128, TI_NMAX = 128, TI_BK = 64, TI_STAGES = 6;
 constexpr int TI_A_BYTES = TI_M * TI_BK * 2;       // 16 KB
-constexpr int TI_B_BYTES = TI_NMAX * TI_BK * 2;    // 32 KB (max)
+constexpr int TI_B_BYTES = TI_NMAX * TI_BK * 2;    // 16 KB (max)
 constexpr int TI_STAGE_BYTES = TI_A_BYTES + TI_B_BYTES;
 constexpr int TI_NEPI = 8;
 constexpr int TI_THREADS = 64 + 32 * TI_NEPI;
@@ -254,7 +254,7 @@ static int tmap(CUtensorMap *m, const void *base, int64_t rows, int K, int box_r
 
 int tc_ivf_launch(const TcIvfLaunch &a, cudaStream_t st) {
     if (a.K % TI_BK) return fail(GN_ERR_INVALID, "tensor-core list scan: K must be a multiple of 64");
-    if (a.x_rows < TI_M || a.q_rows < TI_NMAX) return fail(GN_ERR_INVALID, "tensor-core list scan: buffers too small");
+    if (a.x_rows < TI_M || a.q_rows < 256) return fail(GN_ERR_INVALID, "tensor-core list scan: buffers too small");
     CUtensorMap mx, m32, m64, m128, m256;
     GN_TRY(tmap(&mx, a.X, a.x_rows, a.K, TI_M));
     GN_TRY(tmap(&m32, a.Q, a.q_rows, a.K, 32));
