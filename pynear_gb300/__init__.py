@@ -9,6 +9,7 @@ from .flat import (FlatChebyshevIndex, FlatHammingIndex, FlatL1Index, FlatL2Inde
                    dist_l2)
 from .ivf import IVFFlatBinaryIndex, IVFFlatL2Index, kmeans_l2
 from .prober import LearnedProber
+from .sklearn_adapter import PyNearKNeighborsClassifier, PyNearKNeighborsRegressor, PyNearNearestNeighbors
 
 __version__ = "0.1.0"
 
@@ -17,4 +18,5 @@ __all__ = [
     "VPTreeL2Index", "VPTreeL1Index", "VPTreeChebyshevIndex", "VPTreeBinaryIndex",
     "IVFFlatL2Index", "IVFFlatBinaryIndex", "kmeans_l2", "LearnedProber",
     "dist_l2", "dist_l1", "dist_chebyshev", "dist_hamming",
+    "PyNearNearestNeighbors", "PyNearKNeighborsClassifier", "PyNearKNeighborsRegressor",
 ]

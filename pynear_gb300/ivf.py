@@ -87,6 +87,7 @@ class IVFFlatL2Index:
         or with prober=None go back to the fixed n_probe."""
         from .prober import prob_to_logit
         self._prober = prober  # keeps the model alive while attached
+        self._prober_threshold = float(threshold)
         _lib.call("gn_ivfl2_set_prober", self._h.h, None if prober is None else prober._h.h,
                   prob_to_logit(threshold))
 
@@ -179,12 +180,20 @@ class IVFFlatL2Index:
             for c in range(len(offs) - 1):
                 labels[ids[offs[c]:offs[c + 1]]] = c
             st.update(data=self._data, centroids=cent, labels=labels)
+            prober = getattr(self, "_prober", None)
+            if prober is not None:  # the attached learned prober: weights and threshold
+                st["prober"] = {"params": prober.get_params(), "threshold": self._prober_threshold}
         return st
 
     def __setstate__(self, st):
         self.__init__(st["n_clusters"], st["n_probe"], st.get("engine", "fp32"), st.get("shortlist", 40))
         if st["built"]:
             self.set_assigned(st["data"], st["centroids"], st["labels"])
+            if "prober" in st:
+                from .prober import LearnedProber
+                pr = LearnedProber(self)
+                pr.set_params(st["prober"]["params"])
+                self.set_prober(pr, st["prober"]["threshold"])
 
 
 class IVFFlatBinaryIndex:
@@ -205,6 +214,7 @@ class IVFFlatBinaryIndex:
         n, nb = arr.shape
         _lib.call("gn_ivfbin_set", self._h.h, _lib.ptr(arr), n, nb)
         self._n, self._nbytes = n, nb
+        self._data = arr.copy() if n else None  # host copy for pickling
 
     def search_knn_arrays(self, queries, k: int):
         q = np.ascontiguousarray(queries)
@@ -236,6 +246,18 @@ class IVFFlatBinaryIndex:
 
     def set_nprobe(self, nprobe: int) -> None:
         _lib.call("gn_ivfbin_set_nprobe", self._h.h, int(nprobe))
+
+    # Pickling (the reference's binary IVF has none): the rows and parameters;
+    # the binary k-means is deterministic, so unpickling rebuilds the same
+    # centroids and lists.
+    def __getstate__(self):
+        return {"args": self._args, "data": getattr(self, "_data", None), "nprobe": self.nprobe()}
+
+    def __setstate__(self, st):
+        self.__init__(*st["args"])
+        if st["data"] is not None:
+            self.set(st["data"])
+        self.set_nprobe(st["nprobe"])
 
     def export(self):
         """(centroids (k, nbytes) uint8, labels (n,) int32) of the built index."""
