@@ -235,10 +235,14 @@ def bench_ivf(args, dist, peaks, peak_src):
                 kms += t.value
         return kms
 
+    tuning = {}
+
     def timed(engine, nprobe, steps, warmup, thr=None, graphs=True, profile=False):
         ix.set_engine(engine)
         ix.n_probe = nprobe
         ix.set_prober(prober if thr is not None else None, thr if thr is not None else 0.5)
+        if engine == "tc":  # launch choices per batch-size bucket, timed on 4096 sample queries
+            tuning[(nprobe, thr)] = ix.autotune(tune_q, K).tolist()
         # one captured CUDA graph per batch size, captured during the warm-up
         ix.enable_graphs(nmax if graphs else 0, K)
         for _ in range(warmup):
@@ -290,6 +294,7 @@ def bench_ivf(args, dist, peaks, peak_src):
     t0 = time.perf_counter()
     losses = prober.train(train_q, gt_train, epochs=4, batch=1024, lr=2e-3)
     train_s = time.perf_counter() - t0
+    tune_q = train_q[:4096].copy()  # autotuner sample: training-distribution queries, not the timed ones
     del train_q, gt_train
     learned_cal, thr_sel = [], PROB_THRESHOLDS[-1]
     for thr in PROB_THRESHOLDS:
@@ -376,7 +381,7 @@ def bench_ivf(args, dist, peaks, peak_src):
             "prober": {"train_queries": N_TRAIN, "epochs": 4, "losses": [float(x) for x in losses],
                        "label_s": label_s, "train_s": train_s},
             "calibration": {"fp32": plain_cal, "tc_fixed": tcfix_cal, "learned": learned_cal},
-            "roofline": roofline, "e2e": e2e,
+            "roofline": roofline, "e2e": e2e, "autotune": {str(k): v for k, v in tuning.items()},
             "clocks": clocks, "build_s": build_s, "gen_s": gen_s, "n_batches": len(batches),
             "gpu_launches": launches_per_batch * len(batches) * args.steps,
             "index": (db, cent, offs_l, ids), "eval": ev, "gt_eval": gt_ev}
@@ -584,6 +589,8 @@ def main():
                             "graphs_cached": t["graphs_cached"], "capture_failures": t["graph_capture_failures"],
                             "tuned_without_graphs": ivf["tuned_no_graphs"]["qps"]},
             "tuned_over_plain": t["qps"] / p["qps"], "prober": ivf["prober"],
+            "autotune": {"table_per_bucket": "rows per work unit, most blocks per query selection, selector threads",
+                         "chosen": ivf["autotune"]},
             "roofline": ivf["roofline"], "cpu_baseline": cb, "e2e": ivf["e2e"],
             "gpu_launches": ivf["gpu_launches"], "clocks": ivf["clocks"],
             "build_s": ivf["build_s"], "hamming": ham,

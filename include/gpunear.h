@@ -149,6 +149,16 @@ int gn_ivfl2_enable_graphs(gn_index *ix, int64_t max_batch, int32_t k);
 /* out[0] max_batch (0: disabled), out[1] cached graphs, out[2] replays,
  * out[3] captures that failed (those batches ran uncaptured) */
 int gn_ivfl2_graph_info(gn_index *ix, int64_t *out);
+/* Autotuner of the tensor-core engine (no reference counterpart; results
+ * unchanged): for each batch-size bucket [1,4) [4,16) [16,64) [64,256)
+ * [256,1024) [1024,4096) [4096,..) that the nq sample queries reach, times
+ * every combination of rows per list-scan work unit (256/1024/4096), most
+ * blocks per query selection (1/4/16) and selector threads (128/256), reps
+ * runs each, and keeps the fastest.  table: 7 x {rc, bmax, nt}; zeros = the
+ * built-in choice. */
+int gn_ivfl2_autotune(gn_index *ix, const float *queries, int64_t nq, int64_t k, int32_t reps, int32_t *table_out);
+int gn_ivfl2_get_tuning(gn_index *ix, int32_t *table_out);
+int gn_ivfl2_set_tuning(gn_index *ix, const int32_t *table);
 /* Search engine (no reference counterpart; same result contract):
  *   mode 0  FP32 CUDA-core scan, distances |q|^2 + |x|^2 - 2 q.x clamped at 0,
  *           the formula of forest.py:189-194;

@@ -62,6 +62,9 @@ SIGNATURES = {
     "gn_ivfl2_search_knn_device": [P, P, I64, I64, P, P, P, P],
     "gn_ivfl2_enable_graphs": [P, I64, I32],
     "gn_ivfl2_graph_info": [P, P],
+    "gn_ivfl2_autotune": [P, P, I64, I64, I32, P],
+    "gn_ivfl2_get_tuning": [P, P],
+    "gn_ivfl2_set_tuning": [P, P],
     "gn_ivfl2_set_n_probe": [P, I32],
     "gn_ivfl2_set_mode": [P, I32, I32],
     "gn_ivfl2_error": [P, P],

@@ -40,6 +40,13 @@ struct IvfL2State {
     // learned probing (prober.cu): attached model and logit threshold
     gn_index *prober = nullptr;
     float prober_tau = 0.f;
+    // launch choices of the tensor-core engine per batch-size bucket (ivf_tune.cu):
+    // 0 = built-in heuristic
+    struct TcTune {
+        int32_t rc = 0;    // list rows per work unit (256, 1024, 4096)
+        int32_t bmax = 0;  // most blocks one query's selection is split over (1..16)
+        int32_t nt = 0;    // selector threads per block (128, 256)
+    } tune[7];
     // search configuration version (bumped by every setter); CUDA graphs
     // captured for one configuration are replayed only under it
     uint64_t cfg = 1;
@@ -89,6 +96,12 @@ int ivfl2_coarse_sorted_keys(gn_index *ix, const float *dQ, int64_t nq, int np, 
 int ivfl2_probes(gn_index *ix, const float *dQ, int64_t nq, int *np_out, cudaStream_t st);
 int ivfl2_search_core(gn_index *ix, const float *dQ, int64_t nq, int k, int64_t *d_idx, float *d_dist, int64_t *d_cnt,
                       cudaStream_t st);
+// batch-size bucket of the tuning table: [1,4) [4,16) [16,64) [64,256) [256,1024) [1024,4096) [4096,..)
+inline int tune_bucket(int64_t nq) {
+    int b = 0;
+    for (int64_t x = nq; x >= 4 && b < 6; x >>= 2) ++b;
+    return b;
+}
 // Graph-replayed search; queries/results on the host or the device.
 int ivfl2_search_graph(gn_index *ix, const float *q, bool q_host, int64_t nq, int k, int64_t *idx, float *dist,
                        int64_t *cnt, bool out_host, cudaStream_t user);

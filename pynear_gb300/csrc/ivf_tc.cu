@@ -843,7 +843,8 @@ int ivfl2_search_tc(gn_index *ix, const float *dQ, int64_t nq, int k, int64_t *d
     GN_TRY(ivfl2_probes_tc(ix, dQ, nq, &np, st));
     // work items of rc rows (short items for small batches so that their few
     // lists still spread over all SMs); every pair owns a score segment
-    const int rc = nq >= 64 ? 1024 : 256;
+    const IvfL2State::TcTune &tn = S.tune[tune_bucket(nq)];
+    const int rc = tn.rc ? tn.rc : (nq >= 64 ? 1024 : 256);
     // score segments in 128-row slots: slot_rel / qslot count slots, and a
     // pair's tile t has its minima at tmin4[(slot base + t) * 4 ...]
     GN_TRY(ivf_plan(T, nq, np, S.nc, S.list_off.as<int64_t>(), rc, TC_QCHUNK, st, 128));
@@ -891,8 +892,9 @@ int ivfl2_search_tc(gn_index *ix, const float *dQ, int64_t nq, int k, int64_t *d
     // B blocks per query: split small batches so that they still fill the GPU
     const int nsm = dev_info().num_sms;
     int B = 1;
+    const int bmax = tn.bmax ? tn.bmax : 16;
     if (np <= SEL_PCH)
-        while (B < 16 && nq * B * 2 <= (int64_t)nsm * 4) B *= 2;
+        while (B < bmax && nq * B * 2 <= (int64_t)nsm * 4) B *= 2;
     if (B > 1) {
         // nq * B <= 4 * SMs here: one size for every small batch
         GN_TRY(S.sel_part.ensure((size_t)std::max<int64_t>(nq * B, (int64_t)nsm * 4) * S.shortlist * 8));
@@ -917,7 +919,7 @@ int ivfl2_search_tc(gn_index *ix, const float *dQ, int64_t nq, int k, int64_t *d
             S.sel_part.as<uint64_t>(), S.sel_done.as<int>(), d_idx, d_dist, d_cnt);
         return GN_OK;
     };
-    if (nq * B >= (int64_t)nsm * 8) GN_TRY(sel(std::integral_constant<int, 128>()));
+    if (tn.nt ? tn.nt == 128 : nq * B >= (int64_t)nsm * 8) GN_TRY(sel(std::integral_constant<int, 128>()));
     else GN_TRY(sel(std::integral_constant<int, 256>()));
     GN_CUDA_TRY(cudaGetLastError());
     return GN_OK;

@@ -103,6 +103,27 @@ class IVFFlatL2Index:
         return {"max_batch": int(out[0]), "graphs": int(out[1]), "replays": int(out[2]),
                 "capture_failures": int(out[3])}
 
+    def autotune(self, sample_queries, k: int, reps: int = 3) -> np.ndarray:
+        """Time the tensor-core engine's launch choices on sample queries for
+        every batch-size bucket the sample reaches and keep the fastest; returns
+        the (7, 3) table of (rows per work unit, most blocks per query
+        selection, selector threads) per bucket.  Results are unchanged."""
+        q = _f32_2d(sample_queries, "sample_queries")
+        table = np.zeros((7, 3), np.int32)
+        _lib.call("gn_ivfl2_autotune", self._h.h, _lib.ptr(q), q.shape[0], int(k), int(reps), _lib.ptr(table))
+        return table
+
+    @property
+    def tuning(self) -> np.ndarray:
+        table = np.zeros((7, 3), np.int32)
+        _lib.call("gn_ivfl2_get_tuning", self._h.h, _lib.ptr(table))
+        return table
+
+    @tuning.setter
+    def tuning(self, table) -> None:
+        t = np.ascontiguousarray(table, dtype=np.int32).reshape(7, 3)
+        _lib.call("gn_ivfl2_set_tuning", self._h.h, _lib.ptr(t))
+
     def last_lists_probed(self, nq: int) -> np.ndarray:
         """Lists probed per query by the last search with a prober."""
         out = np.empty(nq, np.int32)
@@ -173,7 +194,7 @@ class IVFFlatL2Index:
 
     def __getstate__(self):
         st = {"n_clusters": self._n_clusters_req, "n_probe": self._n_probe, "built": self._built,
-              "engine": self._engine, "shortlist": self._shortlist}
+              "engine": self._engine, "shortlist": self._shortlist, "tuning": self.tuning}
         if self._built:
             cent, offs, ids = self.export()
             labels = np.empty(self._data.shape[0], np.int32)
@@ -187,6 +208,8 @@ class IVFFlatL2Index:
 
     def __setstate__(self, st):
         self.__init__(st["n_clusters"], st["n_probe"], st.get("engine", "fp32"), st.get("shortlist", 40))
+        if "tuning" in st:
+            self.tuning = st["tuning"]
         if st["built"]:
             self.set_assigned(st["data"], st["centroids"], st["labels"])
             if "prober" in st:
