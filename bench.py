@@ -408,6 +408,130 @@ def cpu_ivf(index, queries, nprobe, budget_s=10.0):
                       f"(restatement of forest.py:63-111,189-194; {threads} threads)"}, dt
 
 
+# ── exact flat L2 (100k x 32, 1,000 queries, k 5) ─────────────────────────
+def bench_flat_l2(args, dist, clocks_mhz):
+    """Exact flat L2 in the reference's arithmetic order; indices checked
+    against the oracle on a 100-query subset."""
+    import torch
+    import pynear_gb300 as gn
+    from pynear_gb300 import _lib, workloads as W
+
+    db, q = W.uniform_l2(n=100_000, d=32, nq=1000, seed=7 + dist.rank)
+    ix = gn.FlatL2Index()
+    ix.set(db)
+    lib = _lib.load()
+    dev = torch.device("cuda", dist.local)
+    stream = torch.cuda.current_stream(dev)
+    d_q = torch.from_numpy(q).to(dev)
+    d_idx = torch.empty((len(q), 5), dtype=torch.int64, device=dev)
+    d_dist = torch.empty((len(q), 5), dtype=torch.float32, device=dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+
+    def step():
+        _lib.check(lib.gn_flat_search_knn_device(ix._h.h, vp(d_q), len(q), 5, vp(d_idx), vp(d_dist),
+                                                 ctypes.c_void_p(stream.cuda_stream)))
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    steps = max(3, args.steps // 2)
+    ms, kern = [], []
+    lib.gn_timing_enable(1)
+    for _ in range(steps):
+        flush.zero_()  # the 12.8 MB database fits in L2
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        step()
+        e1.record(stream)
+        t = ctypes.c_float()
+        _lib.check(lib.gn_timing_last(ctypes.byref(t), None, 0))
+        kern.append(t.value)
+        torch.cuda.synchronize()
+        ms.append(e0.elapsed_time(e1))
+    lib.gn_timing_enable(0)
+    tot = dist.max(sum(ms) / 1e3)
+    import oracle
+    oracle.build()
+    oi, od = oracle.knn_float("l2", db, q[:100], 5)
+    gi = d_idx[:100].cpu().numpy()
+    flops = len(q) * len(db) * 32 * 3  # sub + FMA per element
+    kms = statistics.mean(kern)
+    mhz = clocks_mhz or 2070.0
+    peak = num_sms() * 128 * 2 * mhz * 1e6  # FP32 FMA lanes x 2 flops
+    return {"value": len(q) * steps * dist.ws / tot, "unit": "queries/s", "ms_per_step": statistics.mean(ms),
+            "config": {"n": len(db), "d": 32, "queries_per_step": len(q), "k": 5,
+                       "l2": "flushed between steps (256 MB write)"},
+            "indices_equal_oracle_100q": bool(np.array_equal(gi, oi)),
+            "roofline": {"bound": "fp32", "kernel": "float_scan_kernel", "achieved": flops / (kms / 1e3) / 1e12,
+                         "peak": peak / 1e12, "unit": "TFLOP/s", "frac": flops / (kms / 1e3) / peak,
+                         "kernel_ms": kms, "peak_source": f"derived: 128 FP32 FMA/clk/SM x SMs x {mhz:.0f} MHz",
+                         "note": "latency-bound at this size (12.8 MB database, 1,000 queries)"}}
+
+
+# ── tensor-core shortlist (1M x 128 mixture, 10,000 queries, k 10) ────────
+def bench_tc_shortlist(args, dist, peaks):
+    """BF16 tcgen05 shortlist of 40 + exact FP32 re-rank; recall against the
+    exact GPU scan and the largest distance error against FP64 on a subset."""
+    import torch
+    import pynear_gb300 as gn
+    from pynear_gb300 import _lib, workloads as W
+
+    db, q, _, _ = W.gaussian_mixture(n=1_000_000, d=128, n_centres=1024, sigma=0.3, zipf_s=0, nq=10_000,
+                                     seed=11 + dist.rank)
+    ix = gn.FlatL2TCIndex(shortlist=40)
+    ix.set(db)
+    lib = _lib.load()
+    dev = torch.device("cuda", dist.local)
+    stream = torch.cuda.current_stream(dev)
+    d_q = torch.from_numpy(q).to(dev)
+    d_idx = torch.empty((len(q), K), dtype=torch.int64, device=dev)
+    d_dist = torch.empty((len(q), K), dtype=torch.float32, device=dev)
+
+    def step():
+        _lib.check(lib.gn_tcflat_search_knn_device(ix._h.h, vp(d_q), len(q), K, vp(d_idx), vp(d_dist),
+                                                   ctypes.c_void_p(stream.cuda_stream)))
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    steps = max(3, args.steps // 2)
+    ms, kern = [], []
+    lib.gn_timing_enable(1)
+    for _ in range(steps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        step()
+        e1.record(stream)
+        t = ctypes.c_float()
+        _lib.check(lib.gn_timing_last(ctypes.byref(t), None, 0))
+        kern.append(t.value)
+        torch.cuda.synchronize()
+        ms.append(e0.elapsed_time(e1))
+    lib.gn_timing_enable(0)
+    tot = dist.max(sum(ms) / 1e3)
+    sub = 1000
+    ex = gn.FlatL2Index()
+    ex.set(db)
+    ei, _ = ex.search_knn_arrays(q[:sub], K)
+    del ex
+    gi = d_idx[:sub].cpu().numpy()
+    gd = d_dist[:sub].cpu().numpy().astype(np.float64)
+    recall = recall_at(gi, ei)
+    d64 = np.sqrt(((q[:sub, None, :].astype(np.float64) - db[gi].astype(np.float64)) ** 2).sum(-1))
+    err = float(np.max(np.abs(gd - d64)))
+    flops = 2.0 * 128 * len(db) * len(q)
+    kms = statistics.mean(kern)
+    tc_peak = float(peaks.get("bf16_tflops", 1900.0))
+    return {"value": len(q) * steps * dist.ws / tot, "unit": "queries/s", "ms_per_step": statistics.mean(ms),
+            "config": {"n": len(db), "d": 128, "queries_per_step": len(q), "k": K, "shortlist": 40,
+                       "data": "1,024 N(0,I) centres, sigma 0.3, equal sizes"},
+            "recall_at_10_vs_exact_1000q": recall, "max_abs_dist_err_vs_fp64_1000q": err,
+            "roofline": {"bound": "tensor", "kernel": "tc_topk_kernel",
+                         "achieved": flops / (kms / 1e3) / 1e12, "peak": tc_peak, "unit": "TFLOP/s",
+                         "frac": flops / (kms / 1e3) / 1e12 / tc_peak, "kernel_ms": kms,
+                         "peak_source": "measured (MEASURED_PEAKS.json bf16_tflops, burst)"}}
+
+
 # ── Hamming workload ──────────────────────────────────────────────────────
 def bench_hamming(args, dist, peaks, clocks_mhz):
     import torch
@@ -560,6 +684,8 @@ def main():
     peaks, peak_src = load_peaks()
     ivf = bench_ivf(args, dist, peaks, peak_src)
     ham = bench_hamming(args, dist, peaks, ivf["clocks"].get("sm_mhz"))
+    flat_l2 = bench_flat_l2(args, dist, ivf["clocks"].get("sm_mhz"))
+    tc_short = bench_tc_shortlist(args, dist, peaks)
     cb = None
     if rank == 0 and not args.no_cpu_baseline:
         cb, _ = cpu_ivf(ivf["index"], ivf["eval"], ivf["plain_nprobe"])
@@ -593,7 +719,7 @@ def main():
                          "chosen": ivf["autotune"]},
             "roofline": ivf["roofline"], "cpu_baseline": cb, "e2e": ivf["e2e"],
             "gpu_launches": ivf["gpu_launches"], "clocks": ivf["clocks"],
-            "build_s": ivf["build_s"], "hamming": ham,
+            "build_s": ivf["build_s"], "hamming": ham, "flat_l2_exact": flat_l2, "tc_shortlist": tc_short,
         }
         print(json.dumps(line))
     dist.close()
