@@ -8,11 +8,12 @@
 //              into a 3-stage shared-memory ring (128-byte swizzle);
 //   warp 1     allocates 512 TMEM columns, one thread issues tcgen05.mma
 //              (M=128, N=256, K=16) into one of two 256-column accumulators;
-//   warps 2-5  epilogue: tcgen05.ld of the accumulator rows of their TMEM lane
-//              quadrant; score = |x|^2 - 2 q.x (exact FP32 |x|^2); each thread
-//              owns one query row and keeps its S best (score, row) keys sorted
-//              in shared memory; a float threshold rejects almost every score
-//              with one compare.
+//   warps 2-9  epilogue: tcgen05.ld of the accumulator rows of their TMEM lane
+//              quadrant, half of the columns each; score = |x|^2 - 2 q.x
+//              (exact FP32 |x|^2); each thread owns one query row and keeps
+//              the S best (score, row) keys of its columns in shared memory
+//              (unsorted, the S-th tracked); a float threshold rejects almost
+//              every score with one compare.
 // At the end of a unit each query's S keys go to its partial slot; the re-rank
 // kernel merges a query's slots, keeps the S best by BF16 score, recomputes
 // their distances exactly in FP32 and returns the k nearest.
@@ -33,21 +34,23 @@
 
 namespace gn {
 
-constexpr int TC_M = 128, TC_N = 256, TC_BK = 64, TC_STAGES = 3;
+constexpr int TC_M = 128, TC_N = 256, TC_BK = 64;
 constexpr int TC_A_BYTES = TC_M * TC_BK * 2;   // 16 KB
 constexpr int TC_B_BYTES = TC_N * TC_BK * 2;   // 32 KB
 constexpr int TC_STAGE_BYTES = TC_A_BYTES + TC_B_BYTES;
-// Epilogue warps: 4 in top-S mode (one per TMEM lane quadrant, each thread
-// owns a query row's list), 8 in store mode (two per quadrant, each covering
-// half of the accumulator's columns).
-__host__ __device__ constexpr int tc_nepi(int S) { return S ? 4 : 8; }
+// Epilogue warps: 8, two per TMEM lane quadrant, each covering half of the
+// accumulator's columns (top-S mode: each thread keeps a query row's list for
+// its half; the halves merge at the end of a unit).
+__host__ __device__ constexpr int tc_nepi(int S) { return 8; }
 __host__ __device__ constexpr int tc_threads(int S) { return 64 + 32 * tc_nepi(S); }
+// pipeline depth: two stages when the lists of S = 64 need the room
+__host__ __device__ constexpr int tc_stages(int S) { return S > 40 ? 2 : 3; }
 
 __host__ __device__ constexpr size_t tc_smem_bytes(int S) {
-    // S == 0 is the store mode: a 32x33 transpose tile per epilogue warp
-    return 1024 /*alignment slack*/ + (size_t)TC_STAGES * TC_STAGE_BYTES +
-           (S ? (size_t)TC_M * S * 8 + (size_t)TC_M * 32 * 5 : (size_t)tc_nepi(S) * 32 * 33 * 4) +
-           (size_t)tc_nepi(S) * 32 * 4 + 256;
+    // S == 0 is the store mode: a 32x33 transpose tile per epilogue warp;
+    // top-S mode: two lists (one per column half) of S keys per query row
+    return 1024 /*alignment slack*/ + (size_t)tc_stages(S) * TC_STAGE_BYTES +
+           (S ? (size_t)2 * TC_M * S * 8 : (size_t)tc_nepi(S) * 32 * 33 * 4) + (size_t)tc_nepi(S) * 32 * 4 + 256;
 }
 
 template <int S>
@@ -58,16 +61,15 @@ __global__ void __launch_bounds__(tc_threads(S), 1)
                    const float *__restrict__ bnorm, const int64_t *__restrict__ arow_slot,
                    uint64_t *__restrict__ part, float *__restrict__ scores, int *__restrict__ err) {
     constexpr bool STORE = (S == 0);
-    constexpr int SL = STORE ? 1 : S;  // list length used for shared-memory layout
+    constexpr int SL = STORE ? 1 : 2 * S;  // list keys per query row (two column halves)
     constexpr int NEPI = tc_nepi(S);
+    constexpr int TC_STAGES = tc_stages(S);
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
     uint8_t *stage_base = smem;
-    uint64_t *lists = reinterpret_cast<uint64_t *>(smem + TC_STAGES * TC_STAGE_BYTES);
-    float *cand_s = reinterpret_cast<float *>(lists + TC_M * SL);        // [32][TC_M]
-    uint8_t *cand_j = reinterpret_cast<uint8_t *>(cand_s + 32 * TC_M);   // [32][TC_M]
+    uint64_t *lists = reinterpret_cast<uint64_t *>(smem + TC_STAGES * TC_STAGE_BYTES);  // [2][S][TC_M]
     float *xpose = reinterpret_cast<float *>(smem + TC_STAGES * TC_STAGE_BYTES);  // store mode: [NEPI][32][33]
-    float *snorm = STORE ? xpose + NEPI * 32 * 33 : reinterpret_cast<float *>(cand_j + 32 * TC_M);
+    float *snorm = STORE ? xpose + NEPI * 32 * 33 : reinterpret_cast<float *>(lists + TC_M * SL);
     uint64_t *bars = reinterpret_cast<uint64_t *>(snorm + NEPI * 32);
     uint64_t *full = bars, *empty = bars + TC_STAGES, *accfull = bars + 2 * TC_STAGES,
              *accempty = bars + 2 * TC_STAGES + 2;
@@ -208,11 +210,16 @@ __global__ void __launch_bounds__(tc_threads(S), 1)
             }
         }
     } else {
-        // ── epilogue: warps 2..5, TMEM lane quadrant = warp % 4 ──
-        // list entry i of query row r lives at lists[i * TC_M + r] (bank-conflict free)
-        const int quad = warp & 3;
+        // ── epilogue: warps 2..9, TMEM lane quadrant = warp % 4, column half =
+        // (warp - 2) / 4; each thread keeps the S best keys of one query row
+        // over its half of the columns at lists[(half * S + i) * TC_M + row]
+        // (bank-conflict free), unsorted with the S-th tracked: a new key
+        // replaces the S-th and a scan of S independent loads finds the next.
+        // At the end of a unit the two halves of a row are merged.
+        const int quad = warp & 3, half = (warp - 2) >> 2;
         const int row = quad * 32 + lane;
-        uint64_t *L = lists + row;
+        __shared__ volatile int pair_ok[8];
+        uint64_t *L = lists + (size_t)half * S * TC_M + row;
         float *sn = snorm + (warp - 2) * 32;
         uint32_t tile_it = 0;
         bool ok = true;
@@ -222,51 +229,60 @@ __global__ void __launch_bounds__(tc_threads(S), 1)
 #pragma unroll 4
             for (int i = 0; i < S; ++i) L[i * TC_M] = KEY_EMPTY;
             uint64_t thr = KEY_EMPTY;
+            int maxpos = 0;
             float thr_f = __int_as_float(0x7f800000);  // +inf
             for (int t = 0; t < ntile; ++t, ++tile_it) {
                 const int b = tile_it & 1;
                 const uint32_t tph = (tile_it >> 1) & 1;
                 const int64_t n0 = un.r0 + (int64_t)t * TC_N;
-                // row norms of this tile's 256 columns, fetched before the wait
-                float nrm[TC_N / 32];
+                // row norms of this warp's 128 columns, fetched before the wait
+                float nrm[TC_N / 64];
 #pragma unroll
-                for (int c = 0; c < TC_N / 32; ++c) {
-                    const int64_t col = n0 + c * 32 + lane;
+                for (int c = 0; c < TC_N / 64; ++c) {
+                    const int64_t col = n0 + (half * (TC_N / 64) + c) * 32 + lane;
                     nrm[c] = col < un.r1 ? __ldg(bnorm + col) : 0.f;
                 }
                 if (!mbar_wait(accfull + b, tph, verr)) { ok = false; break; }
                 tc_fence_after();
 #pragma unroll 1
-                for (int c = 0; c < TC_N / 32; ++c) {
+                for (int cc = 0; cc < TC_N / 64; ++cc) {
+                    const int c = half * (TC_N / 64) + cc;
                     const int64_t col0 = n0 + c * 32;
                     __syncwarp();
-                    sn[lane] = nrm[c];
+                    sn[lane] = nrm[cc];
                     __syncwarp();
                     float acc[32];
                     tmem_ld32(tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(b * TC_N + c * 32), acc);
                     const int nvalid = (int)min((int64_t)32, un.r1 - col0);
-                    // branch-free filter: passing scores go to this thread's
-                    // candidate column in shared memory
-                    int cnt = 0;
+                    // filter: a pass mask from independent compares (four partial
+                    // masks, no serial chain); the rare passing scores are offered
+                    uint32_t pm4[4] = {0u, 0u, 0u, 0u};
 #pragma unroll
                     for (int j = 0; j < 32; ++j) {
-                        const float sc = fmaf(-2.f, acc[j], sn[j]);
-                        const bool pass = (j < nvalid) && (sc <= thr_f);
-                        if (pass) {
-                            cand_s[cnt * TC_M + row] = sc;
-                            cand_j[cnt * TC_M + row] = (uint8_t)j;
-                        }
-                        cnt += pass ? 1 : 0;
+                        acc[j] = fmaf(-2.f, acc[j], sn[j]);
+                        pm4[j & 3] |= (acc[j] <= thr_f ? 1u : 0u) << j;
                     }
-#pragma unroll 1
-                    for (int i = 0; i < cnt; ++i) {
-                        const uint64_t key =
-                            make_key(f2ord(cand_s[i * TC_M + row]), (uint32_t)(col0 + cand_j[i * TC_M + row]));
+                    uint32_t pm = (pm4[0] | pm4[1]) | (pm4[2] | pm4[3]);
+                    if (nvalid < 32) pm &= (1u << nvalid) - 1u;
+                    while (pm) {
+                        const int j = __ffs(pm) - 1;
+                        pm &= pm - 1;
+                        float v = acc[0];
+#pragma unroll
+                        for (int jj = 1; jj < 32; ++jj) v = jj == j ? acc[jj] : v;
+                        const uint64_t key = make_key(f2ord(v), (uint32_t)(col0 + j));
                         if (key < thr) {
-                            int p = S - 1;
-                            while (p > 0 && L[(p - 1) * TC_M] > key) { L[p * TC_M] = L[(p - 1) * TC_M]; --p; }
-                            L[p * TC_M] = key;
-                            thr = L[(S - 1) * TC_M];
+                            L[maxpos * TC_M] = key;
+                            uint64_t mx = 0;
+                            int mp = 0;
+#pragma unroll 8
+                            for (int p = 0; p < S; ++p) {
+                                const uint64_t x = L[p * TC_M];
+                                mp = x > mx ? p : mp;
+                                mx = x > mx ? x : mx;
+                            }
+                            thr = mx;
+                            maxpos = mp;
                             thr_f = (thr == KEY_EMPTY) ? __int_as_float(0x7f800000) : ord2f(key_dist(thr));
                         }
                     }
@@ -275,11 +291,46 @@ __global__ void __launch_bounds__(tc_threads(S), 1)
                 __syncwarp();
                 if (lane == 0) mbar_arrive(accempty + b);
             }
-            if (ok && row < un.na) {
-                uint64_t *dst = part + (arow_slot[un.a0 + row] + un.rch) * S;
+            // merge the two halves of each row (the two warps of a quadrant meet
+            // at a named barrier and agree on whether to go on), then the
+            // first half sorts and writes
+            if (lane == 0) pair_ok[quad * 2 + half] = ok ? 1 : 0;
+            asm volatile("bar.sync %0, 64;" ::"r"(1 + quad) : "memory");
+            ok = pair_ok[quad * 2] && pair_ok[quad * 2 + 1];
+            if (half == 0 && ok) {
+                const uint64_t *L2 = L + (size_t)S * TC_M;
+                for (int i = 0; i < S; ++i) {
+                    const uint64_t key = L2[i * TC_M];
+                    if (key < thr) {
+                        L[maxpos * TC_M] = key;
+                        uint64_t mx = 0;
+                        int mp = 0;
+#pragma unroll 8
+                        for (int p = 0; p < S; ++p) {
+                            const uint64_t x = L[p * TC_M];
+                            mp = x > mx ? p : mp;
+                            mx = x > mx ? x : mx;
+                        }
+                        thr = mx;
+                        maxpos = mp;
+                    }
+                }
+                if (row < un.na) {
+                    for (int i = 1; i < S; ++i) {  // ascending, for the re-rank's merge
+                        const uint64_t key = L[i * TC_M];
+                        int p = i;
+                        while (p > 0 && L[(p - 1) * TC_M] > key) {
+                            L[p * TC_M] = L[(p - 1) * TC_M];
+                            --p;
+                        }
+                        L[p * TC_M] = key;
+                    }
+                    uint64_t *dst = part + (arow_slot[un.a0 + row] + un.rch) * S;
 #pragma unroll 4
-                for (int i = 0; i < S; ++i) dst[i] = L[i * TC_M];
+                    for (int i = 0; i < S; ++i) dst[i] = L[i * TC_M];
+                }
             }
+            asm volatile("bar.sync %0, 64;" ::"r"(1 + quad) : "memory");
         }
     }
     tc_fence_before();
