@@ -11,9 +11,9 @@
 //   warps 2-9  epilogue: tcgen05.ld of the accumulator rows of their TMEM lane
 //              quadrant, half of the columns each; score = |x|^2 - 2 q.x
 //              (exact FP32 |x|^2); each thread owns one query row and keeps
-//              the S best (score, row) keys of its columns in shared memory
-//              (unsorted, the S-th tracked); a float threshold rejects almost
-//              every score with one compare.
+//              the S best (score, row) keys of its columns in a shared-memory
+//              max-heap; a float threshold (the root, and the other half's
+//              root) rejects almost every score with one compare.
 // At the end of a unit each query's S keys go to its partial slot; the re-rank
 // kernel merges a query's slots, keeps the S best by BF16 score, recomputes
 // their distances exactly in FP32 and returns the k nearest.
@@ -43,14 +43,37 @@ constexpr int TC_STAGE_BYTES = TC_A_BYTES + TC_B_BYTES;
 // its half; the halves merge at the end of a unit).
 __host__ __device__ constexpr int tc_nepi(int S) { return 8; }
 __host__ __device__ constexpr int tc_threads(int S) { return 64 + 32 * tc_nepi(S); }
-// pipeline depth: two stages when the lists of S = 64 need the room
-__host__ __device__ constexpr int tc_stages(int S) { return S > 40 ? 2 : 3; }
+// pipeline depth: two stages when the lists of S = 40, 64 need the room
+__host__ __device__ constexpr int tc_stages(int S) { return S > 32 ? 2 : 3; }
 
 __host__ __device__ constexpr size_t tc_smem_bytes(int S) {
     // S == 0 is the store mode: a 32x33 transpose tile per epilogue warp;
     // top-S mode: two lists (one per column half) of S keys per query row
     return 1024 /*alignment slack*/ + (size_t)tc_stages(S) * TC_STAGE_BYTES +
            (S ? (size_t)2 * TC_M * S * 8 : (size_t)tc_nepi(S) * 32 * 33 * 4) + (size_t)tc_nepi(S) * 32 * 4 + 256;
+}
+
+// Max-heap of S keys in a thread's strided shared-memory list (element i at
+// L[i * TC_M]): replace the root (the largest) by a smaller key and sift down.
+__device__ __noinline__ void tc_heap_replace_top(uint64_t *L, int S, uint64_t key) {
+    int i = 0;
+    while (true) {
+        const int c = 2 * i + 1;
+        if (c >= S) break;
+        uint64_t cv = L[c * TC_M];
+        int cm = c;
+        if (c + 1 < S) {
+            const uint64_t c2 = L[(c + 1) * TC_M];
+            if (c2 > cv) {
+                cv = c2;
+                cm = c + 1;
+            }
+        }
+        if (cv <= key) break;
+        L[i * TC_M] = cv;
+        i = cm;
+    }
+    L[i * TC_M] = key;
 }
 
 template <int S>
@@ -213,12 +236,13 @@ __global__ void __launch_bounds__(tc_threads(S), 1)
         // ── epilogue: warps 2..9, TMEM lane quadrant = warp % 4, column half =
         // (warp - 2) / 4; each thread keeps the S best keys of one query row
         // over its half of the columns at lists[(half * S + i) * TC_M + row]
-        // (bank-conflict free), unsorted with the S-th tracked: a new key
-        // replaces the S-th and a scan of S independent loads finds the next.
-        // At the end of a unit the two halves of a row are merged.
+        // (bank-conflict free) as a max-heap: a new key replaces the root (the
+        // S-th best) and sifts down.  At the end of a unit the two halves of a
+        // row are merged.
         const int quad = warp & 3, half = (warp - 2) >> 2;
         const int row = quad * 32 + lane;
         __shared__ volatile int pair_ok[8];
+        __shared__ volatile float pair_thr[2 * TC_M];  // each half's current S-th best score per row
         uint64_t *L = lists + (size_t)half * S * TC_M + row;
         float *sn = snorm + (warp - 2) * 32;
         uint32_t tile_it = 0;
@@ -228,9 +252,10 @@ __global__ void __launch_bounds__(tc_threads(S), 1)
             const int ntile = (int)((un.r1 - un.r0 + TC_N - 1) / TC_N);
 #pragma unroll 4
             for (int i = 0; i < S; ++i) L[i * TC_M] = KEY_EMPTY;
-            uint64_t thr = KEY_EMPTY;
-            int maxpos = 0;
+            uint64_t thr = KEY_EMPTY;  // the heap's root: the S-th best key so far
             float thr_f = __int_as_float(0x7f800000);  // +inf
+            pair_thr[half * TC_M + row] = thr_f;
+            asm volatile("bar.sync %0, 64;" ::"r"(1 + quad) : "memory");  // both halves reset before either reads
             for (int t = 0; t < ntile; ++t, ++tile_it) {
                 const int b = tile_it & 1;
                 const uint32_t tph = (tile_it >> 1) & 1;
@@ -244,6 +269,12 @@ __global__ void __launch_bounds__(tc_threads(S), 1)
                 }
                 if (!mbar_wait(accfull + b, tph, verr)) { ok = false; break; }
                 tc_fence_after();
+                // the other half's S-th best also bounds this row: a key not below
+                // it has S better keys in the other half
+                {
+                    const float other = pair_thr[(half ^ 1) * TC_M + row];
+                    thr_f = fminf(thr_f, other);
+                }
 #pragma unroll 1
                 for (int cc = 0; cc < TC_N / 64; ++cc) {
                     const int c = half * (TC_N / 64) + cc;
@@ -272,18 +303,10 @@ __global__ void __launch_bounds__(tc_threads(S), 1)
                         for (int jj = 1; jj < 32; ++jj) v = jj == j ? acc[jj] : v;
                         const uint64_t key = make_key(f2ord(v), (uint32_t)(col0 + j));
                         if (key < thr) {
-                            L[maxpos * TC_M] = key;
-                            uint64_t mx = 0;
-                            int mp = 0;
-#pragma unroll 8
-                            for (int p = 0; p < S; ++p) {
-                                const uint64_t x = L[p * TC_M];
-                                mp = x > mx ? p : mp;
-                                mx = x > mx ? x : mx;
-                            }
-                            thr = mx;
-                            maxpos = mp;
+                            tc_heap_replace_top(L, S, key);
+                            thr = L[0];
                             thr_f = (thr == KEY_EMPTY) ? __int_as_float(0x7f800000) : ord2f(key_dist(thr));
+                            pair_thr[half * TC_M + row] = thr_f;
                         }
                     }
                 }
@@ -302,17 +325,8 @@ __global__ void __launch_bounds__(tc_threads(S), 1)
                 for (int i = 0; i < S; ++i) {
                     const uint64_t key = L2[i * TC_M];
                     if (key < thr) {
-                        L[maxpos * TC_M] = key;
-                        uint64_t mx = 0;
-                        int mp = 0;
-#pragma unroll 8
-                        for (int p = 0; p < S; ++p) {
-                            const uint64_t x = L[p * TC_M];
-                            mp = x > mx ? p : mp;
-                            mx = x > mx ? x : mx;
-                        }
-                        thr = mx;
-                        maxpos = mp;
+                        tc_heap_replace_top(L, S, key);
+                        thr = L[0];
                     }
                 }
                 if (row < un.na) {
