@@ -508,6 +508,10 @@ def bench_tc_shortlist(args, dist, peaks):
         torch.cuda.synchronize()
         ms.append(e0.elapsed_time(e1))
     lib.gn_timing_enable(0)
+    torch.cuda.profiler.start()  # profiler region: one shortlist step
+    step()
+    torch.cuda.synchronize()
+    torch.cuda.profiler.stop()
     tot = dist.max(sum(ms) / 1e3)
     sub = 1000
     ex = gn.FlatL2Index()
