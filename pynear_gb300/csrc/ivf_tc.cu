@@ -325,7 +325,7 @@ __device__ uint32_t block_kth_u32(const uint32_t *v, int n, int kth, int *hist, 
 // (query, list) pair, the scores of the list's rows in 128-row slots and the
 // minimum score of every 32-row quarter of every slot.  Keys are (score, row),
 // so ties go to the lower row.
-//   threshold  tau = the S-th smallest slot minimum of the block's slots
+//   threshold  tau = the S-th smallest quarter minimum of the block's slots
 //              (radix select): S distinct rows score <= tau, so tau bounds the
 //              query's S-th best score;
 //   sweep      warps take 8 slots at a time (lane l: quarter l % 4 of slot
@@ -396,18 +396,22 @@ __global__ void __launch_bounds__(NT, 1024 / NT) ivf_tc_select_kernel(
         const int bu = (int)max((int64_t)1, min((int64_t)B, all / (2 * S)));
         const int64_t lo = bq < bu ? all * bq / bu : all, hi = bq < bu ? all * (bq + 1) / bu : all;
         if (p0 == 0) {
-            // threshold from the block's first slots (any S of them bound it)
+            // threshold from the quarter minima of the block's first slots (any
+            // S of them are S distinct rows' scores, so they bound it)
             uint32_t *tm = reinterpret_cast<uint32_t *>(wreg);
-            const int na = (int)min(hi - lo, (int64_t)NW * SEL_WB * 2);
+            const int ns = (int)min(hi - lo, (int64_t)NW * SEL_WB / 2);
             int p = 0;
-            for (int i = t; i < na; i += NT) {
+            for (int i = t; i < ns; i += NT) {
                 const int64_t f = lo + i;
                 while (p_tpre[p + 1] <= f) ++p;
                 const uint4 m = __ldg(tmin4 + p_slot[p] + (f - p_tpre[p]));
-                tm[i] = min(min(m.x, m.y), min(m.z, m.w));
+                tm[4 * i] = m.x;
+                tm[4 * i + 1] = m.y;
+                tm[4 * i + 2] = m.z;
+                tm[4 * i + 3] = m.w;
             }
             __syncthreads();
-            tau = block_kth_u32<NT>(tm, na, S, hist, sh);
+            tau = block_kth_u32<NT>(tm, 4 * ns, S, hist, sh);
             wthr = tau == 0xffffffffu ? KEY_EMPTY : make_key(tau, 0xffffffffu);
         }
         int p = 0;  // probe of this lane's slot (monotone over the sweep)
