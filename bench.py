@@ -372,7 +372,9 @@ def bench_ivf(args, dist, peaks, peak_src):
     e2e_s = dist.max(time.perf_counter() - t0)
     e2e = {"value": STEP_QUERIES * args.steps * dist.ws / e2e_s, "unit": "queries/s",
            "h2d_bytes_per_step": int(stepq.nbytes), "d2h_bytes_per_step": int(STEP_QUERIES * K * (8 + 4) + STEP_QUERIES * 8)}
-    launches_per_batch = 13  # BF16 queries, coarse units, coarse scan, coarse+MLP, 5 planning, Qb, units, scan, select
+    # kernels per tuned batch: BF16 queries, coarse units, coarse scan, coarse+MLP, planning (one kernel up
+    # to 16,384 (query, list) pairs with 64 probe candidates per query, else five), Qb, units, scan, select
+    launches_per_step = sum(9 if nb_ * 64 <= 16384 else 13 for nb_ in batches)
     cent, offs_l, ids = ix.export()
     ix.enable_graphs(0, 0)
     return {"tuned": tuned, "plain": plain, "tc_fixed": tcfix, "tuned_no_graphs": tuned_ng,
@@ -383,7 +385,7 @@ def bench_ivf(args, dist, peaks, peak_src):
             "calibration": {"fp32": plain_cal, "tc_fixed": tcfix_cal, "learned": learned_cal},
             "roofline": roofline, "e2e": e2e, "autotune": {str(k): v for k, v in tuning.items()},
             "clocks": clocks, "build_s": build_s, "gen_s": gen_s, "n_batches": len(batches),
-            "gpu_launches": launches_per_batch * len(batches) * args.steps,
+            "gpu_launches": launches_per_step * args.steps,
             "index": (db, cent, offs_l, ids), "eval": ev, "gt_eval": gt_ev}
 
 
@@ -533,6 +535,7 @@ def bench_tc_shortlist(args, dist, peaks):
             "roofline": {"bound": "tensor", "kernel": "tc_topk_kernel",
                          "achieved": flops / (kms / 1e3) / 1e12, "peak": tc_peak, "unit": "TFLOP/s",
                          "frac": flops / (kms / 1e3) / 1e12 / tc_peak, "kernel_ms": kms,
+                         "traffic": profile_traffic("tc_topk_kernel"),
                          "peak_source": "measured (MEASURED_PEAKS.json bf16_tflops, burst)"}}
 
 
