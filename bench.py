@@ -656,7 +656,7 @@ def run_reference(args):
             times.append(time.perf_counter() - t0)
             n_done += len(sub)
     v = n_done / sum(times)
-    return {"metric": METRIC, "impl": "reference", "value": v, "unit": "queries/s", "n_gpus": 0,
+    return {"metric": METRIC, "impl": "reference", "value": v, "unit": "queries/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * statistics.mean(times),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic Gaussian mixture (seeded)",

@@ -678,7 +678,7 @@ __global__ void __launch_bounds__(256) coarse_probe_kernel(const float *__restri
     const __nv_bfloat16 *W3 = reinterpret_cast<const __nv_bfloat16 *>(w.W3);
     // layer 1: thread j = hidden unit j, gathered rows of W1 (loads issued ahead)
     float a = w.b1[j];
-#pragma unroll 16
+#pragma unroll 32
     for (int i = 0; i < NC; ++i) {
         const int c = sc[i];
         const float wv = c >= 0 ? __bfloat162float(W1[(size_t)c * H + j]) : 0.f;
