@@ -645,7 +645,7 @@ def run_reference(args):
     cn = (c * c).sum(1)
     for i in range(0, len(db), 65536):
         labels[i:i + 65536] = T.argmin(cn[None, :] - 2 * x[i:i + 65536] @ c.T, dim=1).numpy()
-    nprobe = 32
+    nprobe = 28  # the plain GPU arm calibrates to nprobe 28 for Recall@10 >= 0.95 on this workload
     times, n_done = [], 0
     for s in range(args.warmup + args.steps):
         n = 256
