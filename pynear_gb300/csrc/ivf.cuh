@@ -30,7 +30,6 @@ struct IvfL2State {
     int mode = 0;                // 0 FP32 CUDA-core scan, 1 BF16 tcgen05 shortlist + exact FP32 re-rank
     int shortlist = 40;
     int K = 0;                   // BF16 row length, round_up(d, 64)
-    int rc_tc = 4096;            // list rows per tensor-core work unit
     DBuf x16;                    // n*K BF16 rows, list order
     DBuf qb, aslot, units, nunits, err, scores;
     DBuf sel_part, sel_done;     // split selection: partial best-S lists, per-query arrival counters

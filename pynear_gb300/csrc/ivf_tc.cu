@@ -1,22 +1,27 @@
 // ivf_tc.cu — tensor-core engine of the float IVF index.
 //
-// Same bucketing and work plan as the FP32 scan (ivf.cu), then:
-//   1. Qb      the BF16 copy of each (query, probe) pair's query, rows grouped by
+//   0. probes  coarse_probe_kernel: BF16 centroid scores (tc_ivf_kernel over
+//              the centroids), radix select of the 64 best, exact FP32
+//              distances, then the first n_probe or the learned prober's
+//              choice (its MLP fused here);
+//   1. plan    the same bucketing and work plan as the FP32 scan (ivf.cu),
+//              score segments in 128-row slots;
+//   2. Qb      the BF16 copy of each (query, probe) pair's query, rows grouped by
 //              list (bucket order), so one TMA box covers a work unit's queries;
-//   2. units   one tensor-core work unit per (list, 128-query chunk, row chunk);
-//   3. scan    tc_ivf_kernel: BF16 tcgen05 GEMM of the list's rows (M = 128
-//              per tile) against the unit's queries (N = 32..256) with FP32
+//   3. units   one tensor-core work unit per (list, row chunk, 128-query chunk);
+//   4. scan    tc_ivf_kernel: BF16 tcgen05 GEMM of the list's rows (M = 128
+//              per tile) against the unit's queries (N = 32..128) with FP32
 //              accumulation; the score |x|^2 - 2 q.x (exact FP32 |x|^2) of
-//              every (pair, row) goes to the pair's segment of a score buffer;
-//   4. select  one warp per query walks its probed lists' segments with a
-//              register top-S (S = shortlist), recomputes the S candidates'
-//              squared L2 exactly in FP32 with a compensated sum (two-product
-//              + two-sum) and returns the k nearest, ties to the lower
+//              every (pair, row) goes to the pair's slots, and the minimum of
+//              every 32-row quarter to the slot's four minima;
+//   5. select  per query: a threshold from the quarter minima, only the
+//              quarters below it are read, the S best keys (S = shortlist) by
+//              radix select, their squared L2 recomputed exactly in FP32 with a
+//              compensated sum, the k nearest returned, ties to the lower
 //              original index.
 // Work units are short (a list holds ~1k rows), so selection is kept out of
 // the tensor-core kernel: a per-unit top-S would pay its warm-up on every
-// unit.
-// Everything stays on the device; the batch has no host round trip.
+// unit.  Everything stays on the device; the batch has no host round trip.
 #include <cuda_bf16.h>
 
 #include <algorithm>
@@ -153,25 +158,6 @@ __device__ __forceinline__ void l2sq_warp_rows(const float *__restrict__ q, cons
 #pragma unroll
     for (int r = 0; r < 2; ++r)
         if (r < n) out[r] = l2_warp_total(s[r], c[r]);
-}
-
-// Ascending bitonic sort of n (power of two) keys in shared memory by the
-// whole block.
-template <int NT>
-__device__ __forceinline__ void block_bitonic_sort(uint64_t *a, int n) {
-    for (int size = 2; size <= n; size <<= 1)
-        for (int stride = size >> 1; stride > 0; stride >>= 1) {
-            for (int i = threadIdx.x; i < (n >> 1); i += NT) {
-                const int lo = 2 * i - (i & (stride - 1)), hi = lo + stride;
-                const bool asc = (lo & size) == 0;
-                const uint64_t x = a[lo], y = a[hi];
-                if ((x > y) == asc) {
-                    a[lo] = y;
-                    a[hi] = x;
-                }
-            }
-            __syncthreads();
-        }
 }
 
 constexpr int SEL_PCH = 256;   // probes staged per pass
