@@ -41,20 +41,6 @@ namespace gn {
 
 constexpr int TC_QCHUNK = 128;  // queries per tensor-core work unit (MMA N <= 128)
 
-// Qb row pos = BF16 row of the query of the pair bucket[pos]; warp per row.
-__global__ void qb_fill_kernel(const uint4 *__restrict__ q16, int K8, int np, const int64_t *__restrict__ bucket,
-                               const int64_t *__restrict__ boff_end, const int64_t *__restrict__ qslot,
-                               const int64_t *__restrict__ slot_rel, uint4 *__restrict__ qb,
-                               int64_t *__restrict__ aslot, int64_t max_pairs) {
-    const int lane = threadIdx.x & 31;
-    const int64_t pos = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-    if (pos >= max_pairs || pos >= *boff_end) return;
-    const int64_t pair = bucket[pos];
-    const int64_t q = pair / np;
-    for (int j = lane; j < K8; j += 32) qb[pos * K8 + j] = q16[q * K8 + j];
-    if (lane == 0) aslot[pos] = qslot[q] + slot_rel[pair];
-}
-
 __device__ __forceinline__ int find_list_tc(const int64_t *item_off, int nc, int64_t item) {
     int lo = 0, hi = nc;
     while (hi - lo > 1) {
@@ -65,10 +51,9 @@ __device__ __forceinline__ int find_list_tc(const int64_t *item_off, int nc, int
     return lo;
 }
 
-__global__ void tc_units_kernel(const int64_t *__restrict__ item_off, int nc, const int64_t *__restrict__ boff,
-                                const int64_t *__restrict__ list_off, int rc, int64_t max_units,
-                                TcUnit *__restrict__ units, int64_t *__restrict__ n_units) {
-    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+__device__ void tc_units_body(int64_t i, const int64_t *__restrict__ item_off, int nc,
+                              const int64_t *__restrict__ boff, const int64_t *__restrict__ list_off, int rc,
+                              int64_t max_units, TcUnit *__restrict__ units, int64_t *__restrict__ n_units) {
     const int64_t total = item_off[nc];
     if (i == 0) *n_units = min(total, max_units);
     if (i >= total || i >= max_units) return;
@@ -89,6 +74,30 @@ __global__ void tc_units_kernel(const int64_t *__restrict__ item_off, int nc, co
     u.rch = (int32_t)rch;
     units[i] = u;
 }
+
+// One launch for both: blocks [0, qb_blocks) fill Qb — row pos = the BF16 row
+// of the query of the pair bucket[pos], warp per row — the rest build the
+// work units.
+__global__ void qb_units_kernel(const uint4 *__restrict__ q16, int K8, int np, const int64_t *__restrict__ bucket,
+                                const int64_t *__restrict__ boff, int nc, const int64_t *__restrict__ qslot,
+                                const int64_t *__restrict__ slot_rel, uint4 *__restrict__ qb,
+                                int64_t *__restrict__ aslot, int64_t max_pairs, unsigned qb_blocks,
+                                const int64_t *__restrict__ item_off, const int64_t *__restrict__ list_off, int rc,
+                                int64_t max_units, TcUnit *__restrict__ units, int64_t *__restrict__ n_units) {
+    if (blockIdx.x < qb_blocks) {
+        const int lane = threadIdx.x & 31;
+        const int64_t pos = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+        if (pos >= max_pairs || pos >= boff[nc]) return;
+        const int64_t pair = bucket[pos];
+        const int64_t q = pair / np;
+        for (int j = lane; j < K8; j += 32) qb[pos * K8 + j] = q16[q * K8 + j];
+        if (lane == 0) aslot[pos] = qslot[q] + slot_rel[pair];
+        return;
+    }
+    const int64_t i = (int64_t)(blockIdx.x - qb_blocks) * blockDim.x + threadIdx.x;
+    tc_units_body(i, item_off, nc, boff, list_off, rc, max_units, units, n_units);
+}
+
 
 // Two-sum of a and b: s = fl(a + b) and its exact rounding error.
 __device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
@@ -842,18 +851,17 @@ int ivfl2_search_tc(gn_index *ix, const float *dQ, int64_t nq, int k, int64_t *d
     const int64_t qb_rows = std::max<int64_t>(npairs, 256);  // >= one 256-row TMA box
     GN_TRY(S.qb.ensure((size_t)qb_rows * S.K * 2));
     GN_TRY(S.aslot.ensure((size_t)npairs * 8));
-    qb_fill_kernel<<<(unsigned)ceil_div(npairs, 8), 256, 0, st>>>(
-        S.q16.as<uint4>(), S.K / 8, np, T.bucket.as<int64_t>(), T.boff.as<int64_t>() + S.nc, T.qslot.as<int64_t>(),
-        T.slot_rel.as<int64_t>(), S.qb.as<uint4>(), S.aslot.as<int64_t>(), npairs);
     const int64_t maxlen = S.top_rows.size() > 1 ? S.top_rows[1] : 0;
     // sized for the shortest row chunk (256) so that a smaller batch never needs more
     const int64_t max_units = (ceil_div(npairs, TC_QCHUNK) + S.nc) * (ceil_div(maxlen, 256) + 1);
     GN_TRY(S.units.ensure((size_t)max_units * sizeof(TcUnit)));
     GN_TRY(S.nunits.ensure(8));
-    tc_units_kernel<<<(unsigned)ceil_div(max_units, 256), 256, 0, st>>>(
-        T.item_off.as<int64_t>(), S.nc, T.boff.as<int64_t>(), S.list_off.as<int64_t>(), rc, max_units,
-        S.units.as<TcUnit>(), S.nunits.as<int64_t>());
-    // score segments: at most the rows of the np largest lists per query
+    const unsigned qb_blocks = (unsigned)ceil_div(npairs, 8);
+    qb_units_kernel<<<qb_blocks + (unsigned)ceil_div(max_units, 256), 256, 0, st>>>(
+        S.q16.as<uint4>(), S.K / 8, np, T.bucket.as<int64_t>(), T.boff.as<int64_t>(), S.nc, T.qslot.as<int64_t>(),
+        T.slot_rel.as<int64_t>(), S.qb.as<uint4>(), S.aslot.as<int64_t>(), npairs, qb_blocks,
+        T.item_off.as<int64_t>(), S.list_off.as<int64_t>(), rc, max_units, S.units.as<TcUnit>(),
+        S.nunits.as<int64_t>());
     // score slots: at most the rows of the np largest lists per query, plus one
     // partial slot per probe
     const int64_t np_eff = std::min<int64_t>(np, (int64_t)S.top_rows.size() - 1);
