@@ -497,8 +497,18 @@ __global__ void __launch_bounds__(NT, 1024 / NT) ivf_tc_select_kernel(
         m = block_radix_select<NT>(wreg, SEL_WB, s_wn, S, sel, hist, sh);
     }
 
-    // exact re-rank of the candidates, two rows per warp at a time
+    // exact re-rank of the candidates, two rows per warp at a time; first every
+    // thread prefetches a share of all candidate rows' 128-byte lines into L2,
+    // so that the warps' row loads do not each wait a full DRAM round trip
     const float *qrow = Q + q * dp;
+    {
+        const int lines = (d * 4 + 127) / 128, nc = min(m, S);
+        for (int i = t; i < nc * lines; i += NT) {
+            const uint64_t c = sel[i / lines];
+            if (c != KEY_EMPTY)
+                asm volatile("prefetch.global.L2 [%0];" ::"l"(X + (int64_t)key_idx(c) * dp + (i % lines) * 32));
+        }
+    }
     for (int r = 2 * warp; r < S; r += 2 * NW) {
         int64_t rows[2];
         int n = 0;
