@@ -136,7 +136,9 @@ int gn_ivfl2_set_assigned(gn_index *ix, const float *data, int64_t n, int64_t d,
 int gn_ivfl2_search_knn(gn_index *ix, const float *queries, int64_t nq, int64_t k, int64_t *out_idx,
                         float *out_dist, int64_t *out_cnt);
 /* device variant: queries [nq x d] row-major on the device; results written
- * to device buffers in stream order (no synchronisation) */
+ * to device buffers in stream order (no synchronisation).  Searches of one
+ * index share its scratch: issue them on one stream, or order them (with
+ * graphs enabled they run on the index's own stream and are ordered) */
 int gn_ivfl2_search_knn_device(gn_index *ix, const float *d_queries, int64_t nq, int64_t k, int64_t *d_idx,
                                float *d_dist, int64_t *d_cnt, void *stream);
 int gn_ivfl2_set_n_probe(gn_index *ix, int32_t n_probe);
