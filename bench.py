@@ -383,6 +383,28 @@ def bench_ivf(args, dist, peaks, peak_src):
                 "tensor": {"achieved_tflops": flops_alg / (kms / 1e3) / 1e12, "peak_tflops": tc_peak,
                            "frac": flops_alg / (kms / 1e3) / 1e12 / tc_peak}}
 
+    # the plain arm's scan on the same 4096-query batch: its FP32 work and rate
+    ix.set_prober(None)
+    ix.set_engine("fp32")
+    ix.n_probe = plain_p
+    _lib.check(lib.gn_ivfl2_search_knn_device(ix._h.h, vp(d_q), nb, K, vp(d_idx), vp(d_dist), vp(d_cnt),
+                                              ctypes.c_void_p(stream.cuda_stream)))
+    lib.gn_timing_enable(1)
+    _lib.check(lib.gn_ivfl2_search_knn_device(ix._h.h, vp(d_q), nb, K, vp(d_idx), vp(d_dist), vp(d_cnt),
+                                              ctypes.c_void_p(stream.cuda_stream)))
+    pt = ctypes.c_float()
+    _lib.check(lib.gn_timing_last(ctypes.byref(pt), None, 0))
+    lib.gn_timing_enable(0)
+    pw = np.zeros(4, np.int64)
+    _lib.check(lib.gn_ivfl2_last_work(ix._h.h, pw.ctypes.data_as(ctypes.c_void_p)))
+    p_flops = 2.0 * IVF_D * float(pw[1])
+    fp32_peak = num_sms() * 128 * 2 * 2070e6
+    plain_scan = {"kernel": "ivf_scan_kernel", "batch_queries": nb, "scored_rows": int(pw[1]),
+                  "kernel_ms": pt.value, "achieved_tflops": p_flops / (pt.value / 1e3) / 1e12,
+                  "fp32_peak_tflops": fp32_peak / 1e12, "frac": p_flops / (pt.value / 1e3) / fp32_peak}
+    ix.set_engine("tc")
+    ix.n_probe = tcfix_p
+
     # e2e through the C ABI with pinned host buffers
     h_q = torch.from_numpy(stepq).pin_memory()
     h_idx = torch.empty((nmax, K), dtype=torch.int64).pin_memory()
@@ -417,6 +439,7 @@ def bench_ivf(args, dist, peaks, peak_src):
                        "label_s": label_s, "train_s": train_s},
             "calibration": {"fp32": plain_cal, "tc_fixed": tcfix_cal, "learned": learned_cal},
             "roofline": roofline, "e2e": e2e, "autotune": {str(k): v for k, v in tuning.items()},
+            "plain_scan": plain_scan,
             "clocks": clocks, "build_s": build_s, "gen_s": gen_s, "n_batches": len(batches),
             "gpu_launches": launches_per_step * args.steps,
             "index": (db, cent, offs_l, ids), "eval": ev, "gt_eval": gt_ev}
@@ -748,7 +771,8 @@ def main():
                        "l2": "index data (3 GB) exceeds L2; no flush", "parallelism": f"replicas x{ws}"},
             "recall_at_10": {"tuned": t["recall_eval"], "plain": p["recall_eval"],
                              "calibration": ivf["calibration"]},
-            "plain": {"value": p["qps"], "ms_per_step": p["ms_per_step"], "nprobe": ivf["plain_nprobe"]},
+            "plain": {"value": p["qps"], "ms_per_step": p["ms_per_step"], "nprobe": ivf["plain_nprobe"],
+                      "scan_roofline_4096q": ivf["plain_scan"]},
             "tc_fixed_nprobe": {"value": ivf["tc_fixed"]["qps"], "nprobe": ivf["tuned_nprobe"],
                                 "recall_at_10": ivf["tc_fixed"]["recall_eval"]},
             "cuda_graphs": {"per_batch": "one captured graph per batch size, replayed",
