@@ -179,6 +179,20 @@ int gn_ivfl2_info(gn_index *ix, int32_t *n_clusters_built, int32_t *n_probe, int
  * (n_clusters_built+1, int64), original ids in list order (n, int64) */
 int gn_ivfl2_export(gn_index *ix, float *centroids, int64_t *offsets, int64_t *ids);
 
+/* ── MIHBinaryIndex (pynear/include/MIH.hpp:58-175,
+ *    pynear/src/PythonBindings.cpp:253-271,468-481) ───────────────────────────
+ * Multi-index hashing: m sub-strings of nbytes/m <= 8 bytes, one hash table
+ * each (built on the host at set()).  A query's candidates are the rows whose
+ * t-th sub-string is within radius/m bits of the query's for some t; they are
+ * verified on the GPU (exact Hamming, top-k by (distance, lower row)),
+ * nearest first; out_cnt < k when fewer rows are candidates.  An empty index
+ * returns no results.  k <= 256. */
+int gn_mih_create(int32_t m, gn_index **out);
+int gn_mih_set(gn_index *ix, const uint8_t *data, int64_t n, int64_t nbytes);
+int gn_mih_search_knn(gn_index *ix, const uint8_t *queries, int64_t nq, int64_t k, int32_t radius, int64_t *out_idx,
+                      int64_t *out_dist, int64_t *out_cnt);
+int gn_mih_info(gn_index *ix, int32_t *m, int64_t *n, int64_t *nbytes);
+
 /* ── learned probing (no reference counterpart) ───────────────────────────
  * An MLP (64 -> 256 -> 256 -> one logit per list; BF16 weights, FP32
  * accumulation at inference) scores a query's 64 nearest lists by the

@@ -172,3 +172,32 @@ def ivfl2_search(db, cent, labels, q, k: int, nprobe: int, threads: int = 0):
     lib().or_ivfl2_search(_p(db), db.shape[0], db.shape[1], _p(cent), cent.shape[0], _p(labels), _p(q), nq, k,
                           nprobe, _p(idx), _p(dist_), _p(cnt), threads)
     return idx, dist_, cnt
+
+
+def mih_search(db, q, k: int, m: int, radius: int):
+    """Multi-index hashing search restated in NumPy (pynear/include/MIH.hpp:96-152):
+    a row is a candidate when one of its m sub-strings (nbytes/m bytes) is within
+    radius // m bits of the query's; the k nearest candidates by exact Hamming
+    distance, ties to the lower row index.  Returns (idx, dist, cnt) padded with
+    -1 / 0.  For small cases (dense n x nq x nbytes work)."""
+    db = np.ascontiguousarray(db, dtype=np.uint8)
+    q = np.ascontiguousarray(q, dtype=np.uint8)
+    n, nbytes = db.shape
+    sub = nbytes // m
+    r_sub = radius // m
+    pc = np.unpackbits(np.arange(256, dtype=np.uint8)[:, None], axis=1).sum(1)
+    x = pc[np.bitwise_xor(q[:, None, :], db[None, :, :])]  # (nq, n, nbytes) bit counts
+    full = x.sum(-1)
+    part = x.reshape(len(q), n, m, sub).sum(-1)  # (nq, n, m)
+    cand = (part <= r_sub).any(-1)
+    idx = np.full((len(q), k), -1, np.int64)
+    dist = np.zeros((len(q), k), np.int64)
+    cnt = np.zeros(len(q), np.int64)
+    for i in range(len(q)):
+        rows = np.nonzero(cand[i])[0]
+        order = np.lexsort((rows, full[i, rows]))[:k]
+        c = len(order)
+        idx[i, :c] = rows[order]
+        dist[i, :c] = full[i, rows[order]]
+        cnt[i] = c
+    return idx, dist, cnt

@@ -8,6 +8,7 @@ from .flat import (FlatChebyshevIndex, FlatHammingIndex, FlatL1Index, FlatL2Inde
                    VPTreeChebyshevIndex, VPTreeL1Index, VPTreeL2Index, dist_chebyshev, dist_hamming, dist_l1,
                    dist_l2)
 from .ivf import IVFFlatBinaryIndex, IVFFlatL2Index, kmeans_l2
+from .mih import MIHBinaryIndex
 from .prober import LearnedProber
 from .sklearn_adapter import PyNearKNeighborsClassifier, PyNearKNeighborsRegressor, PyNearNearestNeighbors
 
@@ -16,7 +17,7 @@ __version__ = "0.1.0"
 __all__ = [
     "FlatL2Index", "FlatL2TCIndex", "FlatL1Index", "FlatChebyshevIndex", "FlatHammingIndex",
     "VPTreeL2Index", "VPTreeL1Index", "VPTreeChebyshevIndex", "VPTreeBinaryIndex",
-    "IVFFlatL2Index", "IVFFlatBinaryIndex", "kmeans_l2", "LearnedProber",
+    "IVFFlatL2Index", "IVFFlatBinaryIndex", "MIHBinaryIndex", "kmeans_l2", "LearnedProber",
     "dist_l2", "dist_l1", "dist_chebyshev", "dist_hamming",
     "PyNearNearestNeighbors", "PyNearKNeighborsClassifier", "PyNearKNeighborsRegressor",
 ]

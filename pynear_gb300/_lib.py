@@ -62,6 +62,10 @@ SIGNATURES = {
     "gn_ivfl2_search_knn_device": [P, P, I64, I64, P, P, P, P],
     "gn_ivfl2_enable_graphs": [P, I64, I32],
     "gn_ivfl2_graph_info": [P, P],
+    "gn_mih_create": [I32, PP],
+    "gn_mih_set": [P, P, I64, I64],
+    "gn_mih_search_knn": [P, P, I64, I64, I32, P, P, P],
+    "gn_mih_info": [P, P, P, P],
     "gn_ivfl2_autotune": [P, P, I64, I64, I32, P],
     "gn_ivfl2_get_tuning": [P, P],
     "gn_ivfl2_set_tuning": [P, P],

@@ -34,7 +34,7 @@ struct HBuf {
     HBuf &operator=(const HBuf &) = delete;
 };
 
-enum IndexKind { K_FLAT = 1, K_IVFL2 = 2, K_IVFBIN = 3, K_TCFLAT = 4, K_PROBER = 5 };
+enum IndexKind { K_FLAT = 1, K_IVFL2 = 2, K_IVFBIN = 3, K_TCFLAT = 4, K_PROBER = 5, K_MIH = 6 };
 
 struct IvfL2State;
 struct IvfBinState;
