@@ -526,6 +526,55 @@ def bench_flat_l2(args, dist, clocks_mhz):
                          "note": "latency-bound at this size (12.8 MB database, 1,000 queries)"}}
 
 
+# ── headless Voronoi raster (3840 x 2160 pixels, 64 and 4096 seeds) ─────────
+def bench_voronoi(args, dist, clocks_mhz):
+    """Nearest-seed raster of a 4K pixel grid on device buffers (ids only), the
+    reference demo's compute at its 64-seed cap and at 4096 seeds; ids checked
+    against the oracle on 8 rows."""
+    import torch
+    import pynear_gb300 as gn
+
+    w, h = 3840, 2160
+    dev = torch.device("cuda", dist.local)
+    stream = torch.cuda.current_stream(dev)
+    xs, ys = gn.voronoi.grid_axes(w, h)
+    d_xs, d_ys = torch.from_numpy(xs).to(dev), torch.from_numpy(ys).to(dev)
+    mhz = clocks_mhz or 2070.0
+    out = {"config": {"width": w, "height": h, "output": "int32 seed id per pixel, device buffer",
+                      "l2": "33 MB output written each step; seeds (<= 32 KB) stay cached"}}
+    for ns in (64, 4096):
+        seeds = np.random.default_rng(ns + dist.rank).random((ns, 2), dtype=np.float32)
+        d_s = torch.from_numpy(seeds).to(dev)
+
+        def step():
+            return gn.voronoi_raster_device(d_s, d_xs, d_ys, stream=stream)
+
+        for _ in range(args.warmup):
+            r = step()
+        torch.cuda.synchronize()
+        steps = max(3, args.steps)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            r = step()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = dist.max(e0.elapsed_time(e1) / steps / 1e3) * 1e3
+        import oracle
+        rows = np.linspace(0, h - 1, 8).astype(np.int64)
+        oi, _ = oracle.voronoi_raster(seeds, xs, ys[rows])
+        pairs = w * h * ns
+        # per pixel-seed pair: subtract, multiply, add, compare = 4 FP32-pipe instructions
+        peak_pairs = num_sms() * 128 * mhz * 1e6 / 4
+        out[f"seeds_{ns}"] = {
+            "value": w * h * dist.ws / (ms / 1e3), "unit": "pixels/s", "ms_per_raster": ms,
+            "ids_equal_oracle_8_rows": bool(np.array_equal(r.ids[rows].cpu().numpy(), oi)),
+            "roofline": {"bound": "fp32 issue", "achieved": pairs / (ms / 1e3) / 1e12, "unit": "T pairs/s",
+                         "peak": peak_pairs / 1e12, "frac": pairs / (ms / 1e3) / peak_pairs,
+                         "peak_source": f"derived: 128 FP32 lanes/clk/SM x SMs x {mhz:.0f} MHz / 4 instr per pair"}}
+    return out
+
+
 # ── tensor-core shortlist (1M x 128 mixture, 10,000 queries, k 10) ────────
 def bench_tc_shortlist(args, dist, peaks):
     """BF16 tcgen05 shortlist of 40 + exact FP32 re-rank; recall against the
@@ -749,6 +798,7 @@ def main():
     ham = bench_hamming(args, dist, peaks, ivf["clocks"].get("sm_mhz"))
     flat_l2 = bench_flat_l2(args, dist, ivf["clocks"].get("sm_mhz"))
     tc_short = bench_tc_shortlist(args, dist, peaks)
+    vor = bench_voronoi(args, dist, ivf["clocks"].get("sm_mhz"))
     cb = None
     if rank == 0 and not args.no_cpu_baseline:
         cb, _ = cpu_ivf(ivf["index"], ivf["eval"], ivf["plain_nprobe"])
@@ -784,6 +834,7 @@ def main():
             "roofline": ivf["roofline"], "cpu_baseline": cb, "e2e": ivf["e2e"],
             "gpu_launches": ivf["gpu_launches"], "clocks": ivf["clocks"],
             "build_s": ivf["build_s"], "hamming": ham, "flat_l2_exact": flat_l2, "tc_shortlist": tc_short,
+            "voronoi_raster": vor,
         }
         print(json.dumps(line))
     dist.close()

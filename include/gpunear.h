@@ -234,6 +234,23 @@ int gn_ivfbin_set_nprobe(gn_index *ix, int32_t nprobe);
 /* copy out centroids (k*nbytes) and labels (n); k_out gets min(nlist, n) */
 int gn_ivfbin_export(gn_index *ix, uint8_t *centroids, int32_t *labels, int32_t *k_out);
 
+/* ── headless Voronoi raster (demo/voronoi.py:84-110) ─────────────────────
+ * Replaces the reference's pixel-grid search1NN (VPTreeL2Index over the
+ * n_seeds 2-D seeds, queried with every pixel (xs[c], ys[r])) and palette
+ * lookup.  seeds: n_seeds x 2 floats (x, y); xs: width floats; ys: height
+ * floats.  Outputs, row-major height x width, each optional (NULL = skip, at
+ * least one given): out_ids the nearest seed (ties to the lower index, the
+ * exact flat search1NN answer), out_dist its L2 distance, out_rgba 4 bytes per
+ * pixel = palette[(id % n_palette)] (palette: n_palette x 4 bytes).  The
+ * _device form takes device pointers and launches on `stream` without
+ * synchronising (seeds 8-byte, palette and out_rgba 4-byte aligned). */
+int gn_voronoi_raster(const float *seeds, int64_t n_seeds, const float *xs, int64_t width, const float *ys,
+                      int64_t height, int32_t *out_ids, float *out_dist, const uint8_t *palette, int64_t n_palette,
+                      uint8_t *out_rgba);
+int gn_voronoi_raster_device(const float *d_seeds, int64_t n_seeds, const float *d_xs, int64_t width,
+                             const float *d_ys, int64_t height, int32_t *d_ids, float *d_dist,
+                             const uint8_t *d_palette, int64_t n_palette, uint8_t *d_rgba, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -201,3 +201,23 @@ def mih_search(db, q, k: int, m: int, radius: int):
         dist[i, :c] = full[i, rows[order]]
         cnt[i] = c
     return idx, dist, cnt
+
+
+def voronoi_raster(seeds, xs, ys):
+    """Voronoi raster restated in NumPy (demo/voronoi.py:93-110, a search1NN of
+    every pixel (xs[c], ys[r]) against the seeds): float32 arithmetic in the
+    reference's L2 order for d = 2 (pynear/include/DistanceFunctions.hpp:185-195,
+    sqrt(rn(rn(dx*dx) + rn(dy*dy))), dx = pixel - seed), nearest seed with ties
+    to the lower index.  Returns (ids int32 (h, w), dist float32 (h, w))."""
+    seeds = np.ascontiguousarray(seeds, dtype=np.float32)
+    xs = np.asarray(xs, np.float32)
+    ys = np.asarray(ys, np.float32)
+    ids = np.empty((len(ys), len(xs)), np.int32)
+    dist = np.empty((len(ys), len(xs)), np.float32)
+    for r, py in enumerate(ys):
+        dx = xs[:, None] - seeds[None, :, 0]
+        dy = py - seeds[:, 1]
+        d = np.sqrt(dx * dx + (dy * dy)[None, :])
+        ids[r] = np.argmin(d, axis=1)
+        dist[r] = d[np.arange(len(xs)), ids[r]]
+    return ids, dist

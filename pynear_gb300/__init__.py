@@ -11,6 +11,7 @@ from .ivf import IVFFlatBinaryIndex, IVFFlatL2Index, kmeans_l2
 from .mih import MIHBinaryIndex
 from .prober import LearnedProber
 from .sklearn_adapter import PyNearKNeighborsClassifier, PyNearKNeighborsRegressor, PyNearNearestNeighbors
+from .voronoi import make_palette, voronoi_raster, voronoi_raster_device, write_png
 
 __version__ = "0.1.0"
 
@@ -20,4 +21,5 @@ __all__ = [
     "IVFFlatL2Index", "IVFFlatBinaryIndex", "MIHBinaryIndex", "kmeans_l2", "LearnedProber",
     "dist_l2", "dist_l1", "dist_chebyshev", "dist_hamming",
     "PyNearNearestNeighbors", "PyNearKNeighborsClassifier", "PyNearKNeighborsRegressor",
+    "voronoi_raster", "voronoi_raster_device", "make_palette", "write_png",
 ]

@@ -89,6 +89,8 @@ SIGNATURES = {
     "gn_ivfbin_get_params": [P, P, P],
     "gn_ivfbin_set_nprobe": [P, I32],
     "gn_ivfbin_export": [P, P, P, P],
+    "gn_voronoi_raster": [P, I64, P, I64, P, I64, P, P, P, I64, P],
+    "gn_voronoi_raster_device": [P, I64, P, I64, P, I64, P, P, P, I64, P, P],
 }
 _RESTYPE = {"gn_last_error": ctypes.c_char_p}
 

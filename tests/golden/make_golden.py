@@ -180,11 +180,34 @@ def ivf_l2():
     save("ivf_l2.npz", **out)
 
 
+def voronoi():
+    # The reference demo's raster (demo/voronoi.py:93-110): pixel grid from
+    # linspace(0, 1) axes, one VPTreeL2Index.search1NN of every pixel against
+    # the seeds.  The last case repeats seeds, so some pixels tie.
+    rng = np.random.default_rng(107)
+    out = {}
+    for tag, w, h, ns in (("a", 97, 61, 16), ("b", 160, 90, 64), ("c", 64, 48, 40)):
+        seeds = rng.random((ns, 2), dtype=np.float32)
+        if tag == "c":
+            seeds[20:] = seeds[:20]
+        xs = np.linspace(0, 1, w, dtype=np.float32)
+        ys = np.linspace(0, 1, h, dtype=np.float32)
+        gx, gy = np.meshgrid(xs, ys)
+        grid = np.column_stack([gx.ravel(), gy.ravel()])
+        t = _pynear.VPTreeL2Index()
+        t.set(seeds)
+        i1, d1 = t.search1NN(grid)
+        out.update({f"{tag}_seeds": seeds, f"{tag}_wh": np.array([w, h], np.int64),
+                    f"{tag}_ids": np.array(i1, np.int32).reshape(h, w),
+                    f"{tag}_dist": np.array(d1, np.float32).reshape(h, w)})
+    save("voronoi.npz", **out)
+
+
+ALL = (float_distances, hamming_kat, vptree_float, vptree_binary, kmeans, ivf_binary, ivf_l2, voronoi)
+
 if __name__ == "__main__":
-    float_distances()
-    hamming_kat()
-    vptree_float()
-    vptree_binary()
-    kmeans()
-    ivf_binary()
-    ivf_l2()
+    # optional arguments name the fixtures to (re)generate; none = all
+    want = set(sys.argv[1:])
+    for fn in ALL:
+        if not want or fn.__name__ in want:
+            fn()

@@ -124,3 +124,48 @@ def test_live_against_reference(oracle):
     l1, c1 = _pynear.kmeans_l2(data, 9, 100, 42)
     l2, c2, _ = oracle.kmeans_l2(data, 9, 100, 42)
     assert np.array_equal(l1, l2) and np.array_equal(c1, c2)
+
+
+def _tie_free_agree(ids, dist, ref_ids, ref_dist, seeds, xs, ys):
+    """Distances bit-exact; ids equal except where the reference's seed is at
+    exactly the same distance (its tree returns either of two tied seeds)."""
+    assert np.array_equal(dist.view(np.uint32), ref_dist.view(np.uint32))
+    r, c = np.nonzero(ids != ref_ids)
+    dx = xs[c] - seeds[ref_ids[r, c], 0]
+    dy = ys[r] - seeds[ref_ids[r, c], 1]
+    assert np.array_equal(np.sqrt(dx * dx + dy * dy), dist[r, c])
+    return len(r)
+
+
+def test_voronoi_raster_matches_reference_demo(oracle):
+    g = golden("voronoi.npz")
+    ties = {}
+    for t in "abc":
+        seeds = g[f"{t}_seeds"]
+        w, h = g[f"{t}_wh"]
+        xs = np.linspace(0, 1, w, dtype=np.float32)
+        ys = np.linspace(0, 1, h, dtype=np.float32)
+        ids, dist = oracle.voronoi_raster(seeds, xs, ys)
+        ties[t] = _tie_free_agree(ids, dist, g[f"{t}_ids"], g[f"{t}_dist"], seeds, xs, ys)
+    # distinct random seeds: no ties; case c repeats seeds 0-19 as 20-39
+    assert ties["a"] == 0 and ties["b"] == 0 and ties["c"] > 0
+
+
+def test_png_writer_and_palette(tmp_path):
+    import zlib
+
+    from pynear_gb300 import voronoi as vr
+
+    pal = vr.make_palette(5)
+    assert pal.shape == (5, 4) and (pal[:, 3] == 255).all() and len({tuple(p) for p in pal}) == 5
+    img = np.random.default_rng(0).integers(0, 256, (7, 5, 4), dtype=np.uint8)
+    path = str(tmp_path / "raster.png")
+    vr.write_png(path, img)
+    blob = open(path, "rb").read()
+    assert blob[:8] == b"\x89PNG\r\n\x1a\n" and blob[12:16] == b"IHDR"
+    w, h = int.from_bytes(blob[16:20], "big"), int.from_bytes(blob[20:24], "big")
+    assert (w, h) == (5, 7)
+    start = blob.index(b"IDAT") + 4
+    n = int.from_bytes(blob[start - 8:start - 4], "big")
+    raw = np.frombuffer(zlib.decompress(blob[start:start + n]), np.uint8).reshape(7, 1 + 5 * 4)
+    assert (raw[:, 0] == 0).all() and np.array_equal(raw[:, 1:].reshape(7, 5, 4), img)
