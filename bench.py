@@ -577,71 +577,87 @@ def bench_voronoi(args, dist, clocks_mhz):
 
 # ── tensor-core shortlist (1M x 128 mixture, 10,000 queries, k 10) ────────
 def bench_tc_shortlist(args, dist, peaks):
-    """BF16 tcgen05 shortlist of 40 + exact FP32 re-rank; recall against the
-    exact GPU scan and the largest distance error against FP64 on a subset."""
+    """Tensor-core shortlist + exact FP32 re-rank, in BF16 (shortlist 40) and
+    FP8 E4M3 with per-row scales (shortlist 56: FP8 scores are coarser);
+    recall against the exact GPU scan and the largest distance error against
+    FP64 on a subset."""
     import torch
     import pynear_gb300 as gn
     from pynear_gb300 import _lib, workloads as W
 
     db, q, _, _ = W.gaussian_mixture(n=1_000_000, d=128, n_centres=1024, sigma=0.3, zipf_s=0, nq=10_000,
                                      seed=11 + dist.rank)
-    ix = gn.FlatL2TCIndex(shortlist=40)
-    ix.set(db)
     lib = _lib.load()
     dev = torch.device("cuda", dist.local)
     stream = torch.cuda.current_stream(dev)
     d_q = torch.from_numpy(q).to(dev)
     d_idx = torch.empty((len(q), K), dtype=torch.int64, device=dev)
     d_dist = torch.empty((len(q), K), dtype=torch.float32, device=dev)
-
-    def step():
-        _lib.check(lib.gn_tcflat_search_knn_device(ix._h.h, vp(d_q), len(q), K, vp(d_idx), vp(d_dist),
-                                                   ctypes.c_void_p(stream.cuda_stream)))
-
-    for _ in range(args.warmup):
-        step()
-    torch.cuda.synchronize()
-    steps = max(3, args.steps // 2)
-    ms, kern = [], []
-    lib.gn_timing_enable(1)
-    for _ in range(steps):
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        step()
-        e1.record(stream)
-        t = ctypes.c_float()
-        _lib.check(lib.gn_timing_last(ctypes.byref(t), None, 0))
-        kern.append(t.value)
-        torch.cuda.synchronize()
-        ms.append(e0.elapsed_time(e1))
-    lib.gn_timing_enable(0)
-    torch.cuda.profiler.start()  # profiler region: one shortlist step
-    step()
-    torch.cuda.synchronize()
-    torch.cuda.profiler.stop()
-    tot = dist.max(sum(ms) / 1e3)
     sub = 1000
     ex = gn.FlatL2Index()
     ex.set(db)
     ei, _ = ex.search_knn_arrays(q[:sub], K)
     del ex
-    gi = d_idx[:sub].cpu().numpy()
-    gd = d_dist[:sub].cpu().numpy().astype(np.float64)
-    recall = recall_at(gi, ei)
-    d64 = np.sqrt(((q[:sub, None, :].astype(np.float64) - db[gi].astype(np.float64)) ** 2).sum(-1))
-    err = float(np.max(np.abs(gd - d64)))
     flops = 2.0 * 128 * len(db) * len(q)
-    kms = statistics.mean(kern)
     tc_peak = float(peaks.get("bf16_tflops", 1900.0))
-    return {"value": len(q) * steps * dist.ws / tot, "unit": "queries/s", "ms_per_step": statistics.mean(ms),
+
+    def measure(shortlist, precision, profile):
+        ix = gn.FlatL2TCIndex(shortlist=shortlist, precision=precision)
+        ix.set(db)
+
+        def step():
+            _lib.check(lib.gn_tcflat_search_knn_device(ix._h.h, vp(d_q), len(q), K, vp(d_idx), vp(d_dist),
+                                                       ctypes.c_void_p(stream.cuda_stream)))
+
+        for _ in range(args.warmup):
+            step()
+        torch.cuda.synchronize()
+        steps = max(3, args.steps // 2)
+        ms, kern = [], []
+        lib.gn_timing_enable(1)
+        for _ in range(steps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            step()
+            e1.record(stream)
+            t = ctypes.c_float()
+            _lib.check(lib.gn_timing_last(ctypes.byref(t), None, 0))
+            kern.append(t.value)
+            torch.cuda.synchronize()
+            ms.append(e0.elapsed_time(e1))
+        lib.gn_timing_enable(0)
+        if profile:
+            torch.cuda.profiler.start()  # profiler region: one shortlist step
+            step()
+            torch.cuda.synchronize()
+            torch.cuda.profiler.stop()
+        tot = dist.max(sum(ms) / 1e3)
+        gi = d_idx[:sub].cpu().numpy()
+        gd = d_dist[:sub].cpu().numpy().astype(np.float64)
+        d64 = np.sqrt(((q[:sub, None, :].astype(np.float64) - db[gi].astype(np.float64)) ** 2).sum(-1))
+        kms = statistics.mean(kern)
+        return {"value": len(q) * steps * dist.ws / tot, "ms_per_step": statistics.mean(ms), "kernel_ms": kms,
+                "shortlist": shortlist, "recall_at_10_vs_exact_1000q": recall_at(gi, ei),
+                "max_abs_dist_err_vs_fp64_1000q": float(np.max(np.abs(gd - d64)))}
+
+    bf = measure(40, "bf16", True)
+    f8 = measure(56, "fp8", False)
+    kms = bf["kernel_ms"]
+    return {"value": bf["value"], "unit": "queries/s", "ms_per_step": bf["ms_per_step"],
             "config": {"n": len(db), "d": 128, "queries_per_step": len(q), "k": K, "shortlist": 40,
                        "data": "1,024 N(0,I) centres, sigma 0.3, equal sizes"},
-            "recall_at_10_vs_exact_1000q": recall, "max_abs_dist_err_vs_fp64_1000q": err,
+            "recall_at_10_vs_exact_1000q": bf["recall_at_10_vs_exact_1000q"],
+            "max_abs_dist_err_vs_fp64_1000q": bf["max_abs_dist_err_vs_fp64_1000q"],
             "roofline": {"bound": "tensor", "kernel": "tc_topk_kernel",
                          "achieved": flops / (kms / 1e3) / 1e12, "peak": tc_peak, "unit": "TFLOP/s",
                          "frac": flops / (kms / 1e3) / 1e12 / tc_peak, "kernel_ms": kms,
                          "traffic": profile_traffic("tc_topk_kernel"),
-                         "peak_source": "measured (MEASURED_PEAKS.json bf16_tflops, burst)"}}
+                         "peak_source": "measured (MEASURED_PEAKS.json bf16_tflops, burst)"},
+            "fp8": dict(f8, unit="queries/s", precision="E4M3, one FP32 scale per row",
+                        roofline={"bound": "tensor", "achieved": flops / (f8["kernel_ms"] / 1e3) / 1e12,
+                                  "peak": 2 * tc_peak, "unit": "TFLOP/s",
+                                  "frac": flops / (f8["kernel_ms"] / 1e3) / 1e12 / (2 * tc_peak),
+                                  "peak_source": "derived: 2 x measured BF16 burst (FP8 dense rate)"})}
 
 
 # ── Hamming workload ──────────────────────────────────────────────────────

@@ -97,7 +97,7 @@ int gn_index_destroy(gn_index *ix);
  * stages: a BF16 tcgen05 GEMM scores |x|^2 - 2 q.x with FP32 accumulation and
  * keeps the `shortlist` best rows per query, then those are re-ranked with the
  * reference's FP32 distance.  Exact whenever the true k nearest rows are inside
- * the shortlist.  Shortlist: 16, 32, 40 or 64; k <= min(32, shortlist).
+ * the shortlist.  Shortlist: 16, 32, 40, 48, 56 or 64; k <= min(32, shortlist).
  * Replaces VPTreeL2Index (pynear/src/PythonBindings.cpp:344-350) for
  * large batches.
  */
@@ -108,6 +108,11 @@ int gn_tcflat_search_knn(gn_index *ix, const float *queries, int64_t nq, int64_t
 /* d_queries: nq rows of round_up(d, 4) floats (zero padded) on the device */
 int gn_tcflat_search_knn_device(gn_index *ix, const float *d_queries, int64_t nq, int64_t k, int64_t *d_idx,
                                 float *d_dist, void *stream);
+/* operand precision of the shortlist GEMM: 0 = BF16 (default), 1 = FP8 E4M3
+ * with one FP32 scale per row (max |x| -> 448), scored as
+ * |x|^2 - 2 s_q s_x (q8 . x8); FP8 takes shortlists of 16 to 56.  May be
+ * called before or after set() (the low-precision copy is rebuilt on the GPU). */
+int gn_tcflat_set_precision(gn_index *ix, int32_t precision);
 /* error word of the last tensor-core launch (nonzero: a bounded wait expired) */
 int gn_tc_error(gn_index *ix, int32_t *err_out);
 

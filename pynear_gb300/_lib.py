@@ -53,6 +53,7 @@ SIGNATURES = {
     "gn_tcflat_set": [P, P, I64, I64],
     "gn_tcflat_search_knn": [P, P, I64, I64, P, P],
     "gn_tcflat_search_knn_device": [P, P, I64, I64, P, P, P],
+    "gn_tcflat_set_precision": [P, I32],
     "gn_tc_error": [P, P],
     "gn_kmeans_l2": [P, I64, I64, I64, I64, U32, P, P, P],
     "gn_ivfl2_create": [I32, I32, PP],

@@ -9,8 +9,12 @@
 // other warps through a 4-slot ring of mbarriers:
 //   warp 0     TMA: per 64-wide K slice, 128 list rows (BF16) and the unit's
 //              N query rows (BF16, bucket order) into a 3-stage ring;
-//   warp 1     TMEM (2 x 256 columns) and tcgen05.mma M=128, N, K=16;
-//   warps 2-9  epilogue: thread = list row; for each query column its score
+//   warp 1     TMEM (4 accumulators x 128 columns) and tcgen05.mma M=128, N, K=16;
+//   warps 2-17 epilogue, two sets of eight: set e takes the tiles whose
+//              accumulator index is odd (e = 1) or even (e = 0), so two tiles
+//              are drained at once (the drain is latency-bound: more warps in
+//              flight hide the TMEM-load, shuffle and reduction latencies);
+//              within a set, thread = list row; for each query column its score
 //              |x|^2 - 2 q.x (exact FP32 |x|^2) goes to that (query, probe)
 //              pair's segment at the row's offset — 32 lanes write 32
 //              consecutive rows, so every store is one 128-byte line — and,
@@ -30,10 +34,12 @@ constexpr int TI_M = 128, TI_NMAX = 128, TI_BK = 64, TI_STAGES = 6;
 constexpr int TI_A_BYTES = TI_M * TI_BK * 2;       // 16 KB
 constexpr int TI_B_BYTES = TI_NMAX * TI_BK * 2;    // 16 KB (max)
 constexpr int TI_STAGE_BYTES = TI_A_BYTES + TI_B_BYTES;
-constexpr int TI_NEPI = 8;
+constexpr int TI_NEPI = 16;   // epilogue warps: two sets of eight
+constexpr int TI_SET = 8;     // warps per set (4 TMEM lane quadrants x 2 column groups)
+constexpr int TI_NACC = 4;    // TMEM accumulators of TI_NMAX columns
 constexpr int TI_THREADS = 64 + 32 * TI_NEPI;
 constexpr int TI_UR = 4;  // ring of unit indices handed from the producer to the MMA and epilogue warps
-constexpr size_t TI_SMEM = 1024 + (size_t)TI_STAGES * TI_STAGE_BYTES + 256;
+constexpr size_t TI_SMEM = 1024 + (size_t)TI_STAGES * TI_STAGE_BYTES + 512;
 
 // order-preserving map of a float to an unsigned key
 __device__ __forceinline__ uint32_t ti_ord(float f) {
@@ -54,9 +60,9 @@ __global__ void __launch_bounds__(TI_THREADS, 1)
     uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
     uint64_t *bars = reinterpret_cast<uint64_t *>(smem + TI_STAGES * TI_STAGE_BYTES);
     uint64_t *full = bars, *empty = bars + TI_STAGES, *accfull = bars + 2 * TI_STAGES,
-             *accempty = bars + 2 * TI_STAGES + 2;
-    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 2 * TI_STAGES + 4);
-    uint64_t *ufull = bars + 2 * TI_STAGES + 5, *uempty = ufull + TI_UR;
+             *accempty = bars + 2 * TI_STAGES + TI_NACC;
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 2 * TI_STAGES + 2 * TI_NACC);
+    uint64_t *ufull = bars + 2 * TI_STAGES + 2 * TI_NACC + 1, *uempty = ufull + TI_UR;
     volatile int64_t *uring = reinterpret_cast<volatile int64_t *>(uempty + TI_UR);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     volatile int *verr = err;
@@ -66,9 +72,9 @@ __global__ void __launch_bounds__(TI_THREADS, 1)
             mbar_init(full + s, 1);
             mbar_init(empty + s, 1);
         }
-        for (int b = 0; b < 2; ++b) {
+        for (int b = 0; b < TI_NACC; ++b) {
             mbar_init(accfull + b, 1);
-            mbar_init(accempty + b, TI_NEPI);
+            mbar_init(accempty + b, TI_SET);  // drained by one set
         }
         for (int r = 0; r < TI_UR; ++r) {
             mbar_init(ufull + r, 1);
@@ -130,8 +136,8 @@ __global__ void __launch_bounds__(TI_THREADS, 1)
                 const uint32_t idesc = idesc_bf16_f32(TI_M, nsel);
                 const int ntile = (int)((un.r1 - un.r0 + TI_M - 1) / TI_M);
                 for (int t = 0; t < ntile && ok; ++t, ++tile_it) {
-                    const int b = tile_it & 1;
-                    const uint32_t tph = (tile_it >> 1) & 1;
+                    const int b = tile_it % TI_NACC;
+                    const uint32_t tph = (tile_it / TI_NACC) & 1;
                     if (!mbar_wait(accempty + b, tph ^ 1, verr)) { ok = false; break; }
                     tc_fence_after();
                     const uint32_t dt = tmem + (uint32_t)(b * TI_NMAX);
@@ -153,7 +159,8 @@ __global__ void __launch_bounds__(TI_THREADS, 1)
         }
     } else {
         const int quad = warp & 3;
-        const int grp = (warp - 2) >> 2;  // column chunks grp, grp + 2, ...
+        const int set = (warp - 2) / TI_SET;      // tiles whose accumulator index has parity `set`
+        const int grp = ((warp - 2) >> 2) & 1;    // column chunks grp, grp + 2, ...
         uint32_t tile_it = 0;
         bool ok = true;
         for (uint32_t ui = 0; ok; ++ui) {
@@ -175,8 +182,9 @@ __global__ void __launch_bounds__(TI_THREADS, 1)
             }
             const int ntile = (int)((un.r1 - un.r0 + TI_M - 1) / TI_M);
             for (int t = 0; t < ntile; ++t, ++tile_it) {
-                const int b = tile_it & 1;
-                const uint32_t tph = (tile_it >> 1) & 1;
+                const int b = tile_it % TI_NACC;
+                if ((b & 1) != set) continue;  // the other set's tile
+                const uint32_t tph = (tile_it / TI_NACC) & 1;
                 const int64_t row = un.r0 + (int64_t)t * TI_M + quad * 32 + lane;
                 const bool rok = row < un.r1;
                 const float xn = rok ? __ldg(xnorm + row) : 0.f;

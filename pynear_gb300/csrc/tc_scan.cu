@@ -2,22 +2,30 @@
 // fused per-query top-S epilogue, and the exact FP32 re-rank that follows it.
 //
 // One persistent CTA per SM walks a list of work units.  A unit is a tile of up
-// to 128 "A" rows (queries, BF16) against a range [r0, r1) of "B" rows
-// (database rows, BF16), both K-major with K padded to a multiple of 64.
-//   warp 0     TMA producer: 64-wide K slices of A (128 rows) and B (256 rows)
-//              into a 3-stage shared-memory ring (128-byte swizzle);
+// to 128 "A" rows (queries) against a range [r0, r1) of "B" rows (database
+// rows), both K-major, in one of two precisions:
+//   BF16       K padded to a multiple of 64 elements;
+//   FP8 E4M3   with one FP32 scale per row (row = scale x E4M3 values, the
+//              row's largest magnitude mapped to 448), K padded to 128;
+// either way a pipeline stage holds 128 bytes of K per row.
+//   warp 0     TMA producer: 128-byte K slices of A (128 rows) and B (256 rows)
+//              into a 2- or 3-stage shared-memory ring (128-byte swizzle);
 //   warp 1     allocates 512 TMEM columns, one thread issues tcgen05.mma
-//              (M=128, N=256, K=16) into one of two 256-column accumulators;
+//              (M=128, N=256, K=16 BF16 or K=32 FP8) into one of two
+//              256-column accumulators;
 //   warps 2-9  epilogue: tcgen05.ld of the accumulator rows of their TMEM lane
 //              quadrant, half of the columns each; score = |x|^2 - 2 q.x
-//              (exact FP32 |x|^2); each thread owns one query row and keeps
-//              the S best (score, row) keys of its columns in a shared-memory
-//              max-heap; a float threshold (the root, and the other half's
-//              root) rejects almost every score with one compare.
+//              (exact FP32 |x|^2; FP8: q.x = scale_q scale_x acc); each thread
+//              owns one query row and keeps the S best (score, row) keys of its
+//              columns in a shared-memory max-heap.  A block of 32 scores is
+//              first reduced to its minimum, which is compared with the
+//              threshold (the heap's root, and the other half's root): most
+//              blocks end there, the rest are filtered score by score.
 // At the end of a unit each query's S keys go to its partial slot; the re-rank
 // kernel merges a query's slots, keeps the S best by BF16 score, recomputes
 // their distances exactly in FP32 and returns the k nearest.
 #include <cuda_bf16.h>
+#include <cuda_fp8.h>
 
 #include <algorithm>
 #include <cstring>
@@ -34,7 +42,8 @@
 
 namespace gn {
 
-constexpr int TC_M = 128, TC_N = 256, TC_BK = 64;
+constexpr int TC_M = 128, TC_N = 256, TC_BK = 64;  // TC_BK: BF16 elements per 128-byte K slice
+constexpr int TC_BK8 = 128;                          // FP8 elements per 128-byte K slice
 constexpr int TC_A_BYTES = TC_M * TC_BK * 2;   // 16 KB
 constexpr int TC_B_BYTES = TC_N * TC_BK * 2;   // 32 KB
 constexpr int TC_STAGE_BYTES = TC_A_BYTES + TC_B_BYTES;
@@ -46,11 +55,13 @@ __host__ __device__ constexpr int tc_threads(int S) { return 64 + 32 * tc_nepi(S
 // pipeline depth: two stages when the lists of S = 40, 64 need the room
 __host__ __device__ constexpr int tc_stages(int S) { return S > 32 ? 2 : 3; }
 
-__host__ __device__ constexpr size_t tc_smem_bytes(int S) {
+__host__ __device__ constexpr size_t tc_smem_bytes(int S, bool f8 = false) {
     // S == 0 is the store mode: a 32x33 transpose tile per epilogue warp;
-    // top-S mode: two lists (one per column half) of S keys per query row
+    // top-S mode: two lists (one per column half) of S keys per query row;
+    // per epilogue warp 32 column norms (and, FP8, 32 column scales)
     return 1024 /*alignment slack*/ + (size_t)tc_stages(S) * TC_STAGE_BYTES +
-           (S ? (size_t)2 * TC_M * S * 8 : (size_t)tc_nepi(S) * 32 * 33 * 4) + (size_t)tc_nepi(S) * 32 * 4 + 256;
+           (S ? (size_t)2 * TC_M * S * 8 : (size_t)tc_nepi(S) * 32 * 33 * 4) +
+           (size_t)tc_nepi(S) * 32 * 4 * (f8 ? 2 : 1) + 256;
 }
 
 // Max-heap of S keys in a thread's strided shared-memory list (element i at
@@ -76,14 +87,16 @@ __device__ __noinline__ void tc_heap_replace_top(uint64_t *L, int S, uint64_t ke
     L[i * TC_M] = key;
 }
 
-template <int S>
+template <int S, bool F8>
 __global__ void __launch_bounds__(tc_threads(S), 1)
     tc_topk_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                    const TcUnit *__restrict__ units, const int64_t *__restrict__ n_units_ptr,
-                   const int64_t *__restrict__ cta_off, int K,
-                   const float *__restrict__ bnorm, const int64_t *__restrict__ arow_slot,
+                   const int64_t *__restrict__ cta_off, int K, int kblk,
+                   const float *__restrict__ bnorm, const float *__restrict__ ascale,
+                   const float *__restrict__ bscale, const int64_t *__restrict__ arow_slot,
                    uint64_t *__restrict__ part, float *__restrict__ scores, int *__restrict__ err) {
     constexpr bool STORE = (S == 0);
+    static_assert(!(STORE && F8), "the store mode is BF16 only");
     constexpr int SL = STORE ? 1 : 2 * S;  // list keys per query row (two column halves)
     constexpr int NEPI = tc_nepi(S);
     constexpr int TC_STAGES = tc_stages(S);
@@ -93,7 +106,8 @@ __global__ void __launch_bounds__(tc_threads(S), 1)
     uint64_t *lists = reinterpret_cast<uint64_t *>(smem + TC_STAGES * TC_STAGE_BYTES);  // [2][S][TC_M]
     float *xpose = reinterpret_cast<float *>(smem + TC_STAGES * TC_STAGE_BYTES);  // store mode: [NEPI][32][33]
     float *snorm = STORE ? xpose + NEPI * 32 * 33 : reinterpret_cast<float *>(lists + TC_M * SL);
-    uint64_t *bars = reinterpret_cast<uint64_t *>(snorm + NEPI * 32);
+    float *sscale = snorm + NEPI * 32;  // FP8: per-warp column scales
+    uint64_t *bars = reinterpret_cast<uint64_t *>(snorm + NEPI * 32 * (F8 ? 2 : 1));
     uint64_t *full = bars, *empty = bars + TC_STAGES, *accfull = bars + 2 * TC_STAGES,
              *accempty = bars + 2 * TC_STAGES + 2;
     uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 2 * TC_STAGES + 4);
@@ -126,7 +140,7 @@ __global__ void __launch_bounds__(tc_threads(S), 1)
         u_end = cta_off[blockIdx.x + 1];
         u_step = 1;
     }
-    const int nk = K / TC_BK;
+    const int nk = K / kblk;
 
     if (warp == 0) {
         // ── TMA producer ──
@@ -143,15 +157,15 @@ __global__ void __launch_bounds__(tc_threads(S), 1)
                         if (!mbar_wait(empty + s, ph ^ 1, verr)) { ok = false; break; }
                         uint8_t *sa = stage_base + s * TC_STAGE_BYTES;
                         mbar_expect_tx(full + s, TC_STAGE_BYTES);
-                        tma_load_2d(sa, &tmA, kb * TC_BK, (int)un.a0, full + s);
-                        tma_load_2d(sa + TC_A_BYTES, &tmB, kb * TC_BK, (int)(un.r0 + (int64_t)t * TC_N), full + s);
+                        tma_load_2d(sa, &tmA, kb * kblk, (int)un.a0, full + s);
+                        tma_load_2d(sa + TC_A_BYTES, &tmB, kb * kblk, (int)(un.r0 + (int64_t)t * TC_N), full + s);
                     }
             }
         }
     } else if (warp == 1) {
         // ── MMA issuer ──
         if (lane == 0) {
-            const uint32_t idesc = idesc_bf16_f32(TC_M, TC_N);
+            const uint32_t idesc = F8 ? idesc_e4m3_f32(TC_M, TC_N) : idesc_bf16_f32(TC_M, TC_N);
             uint32_t it = 0, tile_it = 0;
             bool ok = true;
             for (int64_t u = u_begin; u < u_end && ok; u += u_step) {
@@ -170,9 +184,13 @@ __global__ void __launch_bounds__(tc_threads(S), 1)
                         tc_fence_after();
                         const uint32_t sa = smem_u32(stage_base + s * TC_STAGE_BYTES);
                         const uint64_t da = sdesc_sw128(sa), db = sdesc_sw128(sa + TC_A_BYTES);
+                        // four MMAs of 32 bytes of K each (16 BF16 or 32 FP8 elements):
+                        // the descriptors advance by 32 bytes (2 in 16-byte units)
 #pragma unroll
-                        for (int kk = 0; kk < TC_BK / 16; ++kk)
-                            umma_bf16(dt, da + 2 * kk, db + 2 * kk, idesc, (kb | kk) ? 1u : 0u);
+                        for (int kk = 0; kk < 4; ++kk) {
+                            if constexpr (F8) umma_f8(dt, da + 2 * kk, db + 2 * kk, idesc, (kb | kk) ? 1u : 0u);
+                            else umma_bf16(dt, da + 2 * kk, db + 2 * kk, idesc, (kb | kk) ? 1u : 0u);
+                        }
                         umma_commit(empty + s);
                     }
                     if (ok) umma_commit(accfull + b);
@@ -242,9 +260,12 @@ __global__ void __launch_bounds__(tc_threads(S), 1)
         const int quad = warp & 3, half = (warp - 2) >> 2;
         const int row = quad * 32 + lane;
         __shared__ volatile int pair_ok[8];
-        __shared__ volatile float pair_thr[2 * TC_M];  // each half's current S-th best score per row
         uint64_t *L = lists + (size_t)half * S * TC_M + row;
+        // the other half's heap root (its current S-th best key of this row):
+        // only ever holds final root values, so it can be read at any time
+        const volatile uint64_t *other_root = lists + (size_t)(half ^ 1) * S * TC_M + row;
         float *sn = snorm + (warp - 2) * 32;
+        float *sc = sscale + (warp - 2) * 32;
         uint32_t tile_it = 0;
         bool ok = true;
         for (int64_t u = u_begin; u < u_end && ok; u += u_step) {
@@ -254,45 +275,72 @@ __global__ void __launch_bounds__(tc_threads(S), 1)
             for (int i = 0; i < S; ++i) L[i * TC_M] = KEY_EMPTY;
             uint64_t thr = KEY_EMPTY;  // the heap's root: the S-th best key so far
             float thr_f = __int_as_float(0x7f800000);  // +inf
-            pair_thr[half * TC_M + row] = thr_f;
+            // score = |x|^2 + qc * (column factor) * acc: qc = -2 (BF16) or
+            // -2 scale_q (FP8, column factor scale_x)
+            const float qc = F8 ? (row < un.na ? -2.f * __ldg(ascale + un.a0 + row) : 0.f) : -2.f;
             asm volatile("bar.sync %0, 64;" ::"r"(1 + quad) : "memory");  // both halves reset before either reads
             for (int t = 0; t < ntile; ++t, ++tile_it) {
                 const int b = tile_it & 1;
                 const uint32_t tph = (tile_it >> 1) & 1;
                 const int64_t n0 = un.r0 + (int64_t)t * TC_N;
                 // row norms of this warp's 128 columns, fetched before the wait
-                float nrm[TC_N / 64];
+                float nrm[TC_N / 64], csc[TC_N / 64];
 #pragma unroll
                 for (int c = 0; c < TC_N / 64; ++c) {
                     const int64_t col = n0 + (half * (TC_N / 64) + c) * 32 + lane;
                     nrm[c] = col < un.r1 ? __ldg(bnorm + col) : 0.f;
+                    if constexpr (F8) csc[c] = col < un.r1 ? __ldg(bscale + col) : 0.f;
                 }
                 if (!mbar_wait(accfull + b, tph, verr)) { ok = false; break; }
                 tc_fence_after();
                 // the other half's S-th best also bounds this row: a key not below
                 // it has S better keys in the other half
                 {
-                    const float other = pair_thr[(half ^ 1) * TC_M + row];
-                    thr_f = fminf(thr_f, other);
+                    const uint64_t o = *other_root;
+                    if (o != KEY_EMPTY) thr_f = fminf(thr_f, ord2f(key_dist(o)));
                 }
 #pragma unroll 1
                 for (int cc = 0; cc < TC_N / 64; ++cc) {
                     const int c = half * (TC_N / 64) + cc;
                     const int64_t col0 = n0 + c * 32;
+                    // columns past the unit's last row (the tail of its last tile,
+                    // TMA zero fill) are never offered; col0 is warp-uniform
+                    if (col0 >= un.r1) break;
                     __syncwarp();
                     sn[lane] = nrm[cc];
+                    if constexpr (F8) sc[lane] = csc[cc];
                     __syncwarp();
                     float acc[32];
                     tmem_ld32(tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(b * TC_N + c * 32), acc);
-                    const int nvalid = (int)min((int64_t)32, un.r1 - col0);
+                    // scores and their minimum (four independent chains)
+                    const float4 *sn4 = reinterpret_cast<const float4 *>(sn);
+                    const float4 *sc4 = reinterpret_cast<const float4 *>(sc);
+                    const float inf = __int_as_float(0x7f800000);
+                    float mn4[4] = {inf, inf, inf, inf};
+#pragma unroll
+                    for (int j4 = 0; j4 < 8; ++j4) {
+                        const float4 nv = sn4[j4];
+                        float4 cf = make_float4(qc, qc, qc, qc);
+                        if constexpr (F8) {
+                            const float4 sv = sc4[j4];
+                            cf = make_float4(qc * sv.x, qc * sv.y, qc * sv.z, qc * sv.w);
+                        }
+                        acc[4 * j4 + 0] = fmaf(cf.x, acc[4 * j4 + 0], nv.x);
+                        acc[4 * j4 + 1] = fmaf(cf.y, acc[4 * j4 + 1], nv.y);
+                        acc[4 * j4 + 2] = fmaf(cf.z, acc[4 * j4 + 2], nv.z);
+                        acc[4 * j4 + 3] = fmaf(cf.w, acc[4 * j4 + 3], nv.w);
+                        mn4[0] = fminf(mn4[0], acc[4 * j4 + 0]);
+                        mn4[1] = fminf(mn4[1], acc[4 * j4 + 1]);
+                        mn4[2] = fminf(mn4[2], acc[4 * j4 + 2]);
+                        mn4[3] = fminf(mn4[3], acc[4 * j4 + 3]);
+                    }
+                    if (!(fminf(fminf(mn4[0], mn4[1]), fminf(mn4[2], mn4[3])) <= thr_f)) continue;
+                    const int nvalid = (int)min((int64_t)32, un.r1 - col0);  // 1..32
                     // filter: a pass mask from independent compares (four partial
                     // masks, no serial chain); the rare passing scores are offered
                     uint32_t pm4[4] = {0u, 0u, 0u, 0u};
 #pragma unroll
-                    for (int j = 0; j < 32; ++j) {
-                        acc[j] = fmaf(-2.f, acc[j], sn[j]);
-                        pm4[j & 3] |= (acc[j] <= thr_f ? 1u : 0u) << j;
-                    }
+                    for (int j = 0; j < 32; ++j) pm4[j & 3] |= (acc[j] <= thr_f ? 1u : 0u) << j;
                     uint32_t pm = (pm4[0] | pm4[1]) | (pm4[2] | pm4[3]);
                     if (nvalid < 32) pm &= (1u << nvalid) - 1u;
                     while (pm) {
@@ -306,7 +354,6 @@ __global__ void __launch_bounds__(tc_threads(S), 1)
                             tc_heap_replace_top(L, S, key);
                             thr = L[0];
                             thr_f = (thr == KEY_EMPTY) ? __int_as_float(0x7f800000) : ord2f(key_dist(thr));
-                            pair_thr[half * TC_M + row] = thr_f;
                         }
                     }
                 }
@@ -373,14 +420,17 @@ static EncodeTiledFn encode_tiled() {
     return fn;
 }
 
-static int make_tmap_bf16(CUtensorMap *map, const void *base, int64_t rows, int64_t K, int box_rows) {
+// K-major operand rows of K elements (BF16, or FP8 stored as bytes), boxes of
+// 128 bytes of K by box_rows rows, 128-byte swizzle.
+static int make_tmap_rows(CUtensorMap *map, const void *base, int64_t rows, int64_t K, int box_rows, bool f8) {
     EncodeTiledFn cuTensorMapEncodeTiled = encode_tiled();
     if (!cuTensorMapEncodeTiled) return fail(GN_ERR_CUDA, "cuTensorMapEncodeTiled is unavailable");
     cuuint64_t dims[2] = {(cuuint64_t)K, (cuuint64_t)rows};
-    cuuint64_t strides[1] = {(cuuint64_t)K * 2};
-    cuuint32_t box[2] = {(cuuint32_t)TC_BK, (cuuint32_t)box_rows};
+    cuuint64_t strides[1] = {(cuuint64_t)K * (f8 ? 1 : 2)};
+    cuuint32_t box[2] = {(cuuint32_t)(f8 ? TC_BK8 : TC_BK), (cuuint32_t)box_rows};
     cuuint32_t estr[2] = {1, 1};
-    CUresult r = cuTensorMapEncodeTiled(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void *>(base), dims,
+    CUresult r = cuTensorMapEncodeTiled(map, f8 ? CU_TENSOR_MAP_DATA_TYPE_UINT8 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2,
+                                        const_cast<void *>(base), dims,
                                         strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
                                         CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                                         CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
@@ -389,25 +439,45 @@ static int make_tmap_bf16(CUtensorMap *map, const void *base, int64_t rows, int6
 }
 
 int tc_topk_launch(const TcLaunch &a, cudaStream_t st) {
-    if (a.K % TC_BK) return fail(GN_ERR_INVALID, "tensor-core scan: K must be a multiple of 64");
+    const int kblk = a.fp8 ? TC_BK8 : TC_BK;
+    if (a.K % kblk)
+        return fail(GN_ERR_INVALID, a.fp8 ? "tensor-core scan: FP8 K must be a multiple of 128"
+                                          : "tensor-core scan: K must be a multiple of 64");
+    if (a.fp8 && (a.S == 0 || a.S > 56 || !a.ascale || !a.bscale))
+        return fail(GN_ERR_UNSUPPORTED, "FP8 shortlist: S must be 16, 32, 40, 48 or 56, with row scales");
     CUtensorMap ma, mb;
-    GN_TRY(make_tmap_bf16(&ma, a.A, std::max<int64_t>(a.a_rows, 1), a.K, TC_M));
-    GN_TRY(make_tmap_bf16(&mb, a.B, std::max<int64_t>(a.b_rows, 1), a.K, TC_N));
-    auto launch = [&](auto SC) {
+    GN_TRY(make_tmap_rows(&ma, a.A, std::max<int64_t>(a.a_rows, 1), a.K, TC_M, a.fp8));
+    GN_TRY(make_tmap_rows(&mb, a.B, std::max<int64_t>(a.b_rows, 1), a.K, TC_N, a.fp8));
+    auto launch = [&](auto SC, auto FC) -> int {
         constexpr int Sv = decltype(SC)::value;
-        const size_t smem = tc_smem_bytes(Sv);
-        cudaFuncSetAttribute(tc_topk_kernel<Sv>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        tc_topk_kernel<Sv><<<a.grid, tc_threads(Sv), smem, st>>>(ma, mb, a.units, a.n_units, a.cta_off, a.K, a.bnorm,
-                                                              a.arow_slot, a.part, a.scores, a.err);
+        constexpr bool Fv = decltype(FC)::value;
+        const size_t smem = tc_smem_bytes(Sv, Fv);
+        GN_CUDA_TRY(cudaFuncSetAttribute(tc_topk_kernel<Sv, Fv>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem));
+        tc_topk_kernel<Sv, Fv><<<a.grid, tc_threads(Sv), smem, st>>>(ma, mb, a.units, a.n_units, a.cta_off, a.K,
+                                                                     kblk, a.bnorm, a.ascale, a.bscale, a.arow_slot,
+                                                                     a.part, a.scores, a.err);
         return GN_OK;
     };
+    using F0 = std::false_type;
+    using F1 = std::true_type;
+    if (a.fp8) switch (a.S) {
+        case 16: return launch(std::integral_constant<int, 16>(), F1());
+        case 32: return launch(std::integral_constant<int, 32>(), F1());
+        case 40: return launch(std::integral_constant<int, 40>(), F1());
+        case 48: return launch(std::integral_constant<int, 48>(), F1());
+        case 56: return launch(std::integral_constant<int, 56>(), F1());
+        default: break;
+        }
     switch (a.S) {
-    case 0: return launch(std::integral_constant<int, 0>());
-    case 16: return launch(std::integral_constant<int, 16>());
-    case 32: return launch(std::integral_constant<int, 32>());
-    case 40: return launch(std::integral_constant<int, 40>());
-    case 64: return launch(std::integral_constant<int, 64>());
-    default: return fail(GN_ERR_UNSUPPORTED, "shortlist size must be 16, 32, 40 or 64");
+    case 0: return launch(std::integral_constant<int, 0>(), F0());
+    case 16: return launch(std::integral_constant<int, 16>(), F0());
+    case 32: return launch(std::integral_constant<int, 32>(), F0());
+    case 40: return launch(std::integral_constant<int, 40>(), F0());
+    case 48: return launch(std::integral_constant<int, 48>(), F0());
+    case 56: return launch(std::integral_constant<int, 56>(), F0());
+    case 64: return launch(std::integral_constant<int, 64>(), F0());
+    default: return fail(GN_ERR_UNSUPPORTED, "shortlist size must be 16, 32, 40, 48, 56 or 64");
     }
 }
 
@@ -425,6 +495,33 @@ void to_bf16_rows(const float *X, int64_t n, int d, int ldx, void *out, int K, c
     if (n > 0)
         f32_to_bf16_rows_kernel<<<(unsigned)ceil_div(n * K, 256), 256, 0, st>>>(
             X, n, d, ldx, reinterpret_cast<__nv_bfloat16 *>(out), K);
+}
+
+// FP8 E4M3 rows with one FP32 scale each: warp per row; scale = max|x| / 448
+// (the largest E4M3 magnitude; 1 for an all-zero row), element = x / scale
+// rounded to nearest E4M3 with saturation, zero beyond d up to K.
+__global__ void f32_to_e4m3_rows_kernel(const float *__restrict__ X, int64_t n, int d, int ldx,
+                                        uint8_t *__restrict__ out, float *__restrict__ scale, int K) {
+    const int64_t r = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    const int lane = threadIdx.x & 31;
+    if (r >= n) return;
+    const float *x = X + r * ldx;
+    float m = 0.f;
+    for (int j = lane; j < d; j += 32) m = fmaxf(m, fabsf(x[j]));
+#pragma unroll
+    for (int o = 16; o; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    const float sc = m > 0.f ? m / 448.f : 1.f;
+    const float inv = m > 0.f ? 448.f / m : 1.f;
+    if (lane == 0) scale[r] = sc;
+    uint8_t *o = out + r * K;
+    for (int j = lane; j < K; j += 32)
+        o[j] = j < d ? (uint8_t)__nv_cvt_float_to_fp8(x[j] * inv, __NV_SATFINITE, __NV_E4M3) : (uint8_t)0;
+}
+
+void to_e4m3_rows(const float *X, int64_t n, int d, int ldx, void *out, float *scale, int K, cudaStream_t st) {
+    if (n > 0)
+        f32_to_e4m3_rows_kernel<<<(unsigned)ceil_div(n, 8), 256, 0, st>>>(X, n, d, ldx,
+                                                                          reinterpret_cast<uint8_t *>(out), scale, K);
 }
 
 // ── exact re-rank ─────────────────────────────────────────────────────────
@@ -490,12 +587,31 @@ int tc_rerank_launch(const uint64_t *part, int nslot, int S, const float *Q, con
 struct TcFlatState {
     int d = 0, dp = 0, K = 0;
     int S = 40;
+    int fp8 = 0;  // 0: BF16 operands; 1: FP8 E4M3 with per-row scales
     int64_t n = 0;
-    DBuf x32, x16, xnorm;  // fp32 rows (dp), bf16 rows (K), |x|^2
-    DBuf q32, q16, units, nunits, ctaoff, aslot, part, err, out_idx, out_dist;
+    DBuf x32, x16, xnorm, xscale;  // fp32 rows (dp), low-precision rows (K), |x|^2, FP8 row scales
+    DBuf q32, q16, qscale, units, nunits, ctaoff, aslot, part, err, out_idx, out_dist;
     int64_t planned_nq = -1;
     int nchunks = 1, grid = 0;
 };
+
+// The database's low-precision copy in the index's precision, from its FP32
+// rows; it holds at least one full 256-row TMA box.
+static int tcflat_lowp(TcFlatState &S, cudaStream_t st) {
+    S.K = (int)round_up(S.d, S.fp8 ? TC_BK8 : TC_BK);
+    const size_t bytes = (size_t)std::max<int64_t>(S.n, TC_N) * S.K * (S.fp8 ? 1 : 2);
+    GN_TRY(S.x16.ensure(bytes));
+    GN_CUDA_TRY(cudaMemsetAsync(S.x16.p, 0, bytes, st));
+    if (S.fp8) {
+        GN_TRY(S.xscale.ensure((size_t)S.n * 4));
+        to_e4m3_rows(S.x32.as<float>(), S.n, S.d, S.dp, S.x16.p, S.xscale.as<float>(), S.K, st);
+    } else {
+        S.xscale.release();
+        to_bf16_rows(S.x32.as<float>(), S.n, S.d, S.dp, S.x16.p, S.K, st);
+    }
+    GN_CUDA_TRY(cudaGetLastError());
+    return GN_OK;
+}
 
 // Split the (query tile, database tile) space into one contiguous run per CTA,
 // cut at query-tile boundaries: each CTA keeps its per-query lists over
@@ -556,8 +672,9 @@ extern "C" {
 
 int gn_tcflat_create(int32_t shortlist, gn_index **out) {
     if (!out) return fail(GN_ERR_INVALID, "out is NULL");
-    if (shortlist != 16 && shortlist != 32 && shortlist != 40 && shortlist != 64)
-        return fail(GN_ERR_INVALID, "shortlist must be 16, 32, 40 or 64");
+    if (shortlist != 16 && shortlist != 32 && shortlist != 40 && shortlist != 48 && shortlist != 56 &&
+        shortlist != 64)
+        return fail(GN_ERR_INVALID, "shortlist must be 16, 32, 40, 48, 56 or 64");
     gn_index *ix = new gn_index();
     ix->kind = K_TCFLAT;
     ix->metric = GN_METRIC_L2;
@@ -580,14 +697,10 @@ int gn_tcflat_set(gn_index *ix, const float *data, int64_t n, int64_t d) {
     S.n = n;
     S.d = (int)d;
     S.dp = (int)round_up(d, 4);
-    S.K = (int)round_up(d, TC_BK);
     GN_TRY(upload_rows(S.x32, data, n, d * 4, S.dp / 4, st));
-    // the BF16 copy holds at least one full 256-row TMA box
-    GN_TRY(S.x16.ensure((size_t)std::max<int64_t>(n, TC_N) * S.K * 2));
-    GN_CUDA_TRY(cudaMemsetAsync(S.x16.p, 0, (size_t)std::max<int64_t>(n, TC_N) * S.K * 2, st));
     GN_TRY(S.xnorm.ensure((size_t)n * 4));
-    to_bf16_rows(S.x32.as<float>(), n, S.d, S.dp, S.x16.p, S.K, st);
     row_norms(S.x32.as<float>(), n, S.dp, S.xnorm.as<float>(), st);  // |x|^2 in FP32
+    GN_TRY(tcflat_lowp(S, st));
     GN_TRY(S.err.ensure(4));
     GN_CUDA_TRY(cudaMemsetAsync(S.err.p, 0, 4, st));
     GN_CUDA_TRY(cudaStreamSynchronize(st));
@@ -608,9 +721,14 @@ int gn_tcflat_search_knn_device(gn_index *ix, const float *d_queries, int64_t nq
     std::lock_guard<std::mutex> lk(ix->mu);
     cudaStream_t st = (cudaStream_t)stream;
     if (S.planned_nq != nq) GN_TRY(tcflat_plan(S, nq, st));
-    GN_TRY(S.q16.ensure((size_t)std::max<int64_t>(nq, TC_M) * S.K * 2));  // >= one 128-row TMA box
+    GN_TRY(S.q16.ensure((size_t)std::max<int64_t>(nq, TC_M) * S.K * (S.fp8 ? 1 : 2)));  // >= one 128-row TMA box
     GN_TRY(S.part.ensure((size_t)nq * S.nchunks * S.S * 8));
-    to_bf16_rows(d_queries, nq, S.d, S.dp, S.q16.p, S.K, st);
+    if (S.fp8) {
+        GN_TRY(S.qscale.ensure((size_t)nq * 4));
+        to_e4m3_rows(d_queries, nq, S.d, S.dp, S.q16.p, S.qscale.as<float>(), S.K, st);
+    } else {
+        to_bf16_rows(d_queries, nq, S.d, S.dp, S.q16.p, S.K, st);
+    }
     // slots of a query tile covered by fewer runs than the maximum stay empty
     GN_CUDA_TRY(cudaMemsetAsync(S.part.p, 0xff, (size_t)nq * S.nchunks * S.S * 8, st));
     TcLaunch a;
@@ -628,6 +746,9 @@ int gn_tcflat_search_knn_device(gn_index *ix, const float *d_queries, int64_t nq
     a.err = S.err.as<int>();
     a.S = S.S;
     a.grid = S.grid;
+    a.fp8 = S.fp8;
+    a.ascale = S.fp8 ? S.qscale.as<float>() : nullptr;
+    a.bscale = S.fp8 ? S.xscale.as<float>() : nullptr;
     timing_begin(st, "tc_topk_kernel");
     GN_TRY(tc_topk_launch(a, st));
     timing_end(st);
@@ -661,6 +782,22 @@ int gn_tcflat_search_knn(gn_index *ix, const float *queries, int64_t nq, int64_t
     if (herr) {
         cudaMemset(S.err.p, 0, 4);
         return fail(GN_ERR_TIMEOUT, "tensor-core scan: a pipeline wait timed out");
+    }
+    return GN_OK;
+}
+
+int gn_tcflat_set_precision(gn_index *ix, int32_t precision) {
+    if (!ix || ix->kind != K_TCFLAT) return fail(GN_ERR_INVALID, "not a tensor-core flat index");
+    if (precision != 0 && precision != 1) return fail(GN_ERR_INVALID, "precision must be 0 (BF16) or 1 (FP8 E4M3)");
+    std::lock_guard<std::mutex> lk(ix->mu);
+    TcFlatState &S = *tcs(ix);
+    if (precision == 1 && S.S > 56)
+        return fail(GN_ERR_UNSUPPORTED, "FP8 shortlist: S must be 16, 32, 40, 48 or 56");
+    if (S.fp8 == precision) return GN_OK;
+    S.fp8 = precision;
+    if (S.n > 0) {
+        GN_TRY(tcflat_lowp(S, ix->stream));
+        GN_CUDA_TRY(cudaStreamSynchronize(ix->stream));
     }
     return GN_OK;
 }

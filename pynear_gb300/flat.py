@@ -130,16 +130,27 @@ class FlatHammingIndex(_NearestFirst):
 
 
 class FlatL2TCIndex:
-    """Exact Euclidean k-NN for large batches: BF16 tensor-core shortlist of
+    """Exact Euclidean k-NN for large batches: tensor-core shortlist of
     `shortlist` rows per query (tcgen05 GEMM, FP32 accumulation), re-ranked with
     the reference's FP32 L2 distance.  Results are nearest-first and equal the
     exact scan whenever the true k nearest rows are in the shortlist; k <= 32.
+
+    ``precision``: "bf16" (default) or "fp8" (E4M3 operands with one FP32 scale
+    per row; shortlist 16, 32, 40, 48 or 56 -- FP8 scores are coarser, so
+    a longer shortlist keeps the same recall).
     """
 
-    def __init__(self, shortlist: int = 40) -> None:
+    _PRECISIONS = {"bf16": 0, "fp8": 1}
+
+    def __init__(self, shortlist: int = 40, precision: str = "bf16") -> None:
+        if precision not in self._PRECISIONS:
+            raise ValueError("precision must be 'bf16' or 'fp8'")
         self._h = _lib.Handle("gn_tcflat_create", int(shortlist))
         self._n = 0
         self._dim = 0
+        self.precision = precision
+        if precision != "bf16":
+            _lib.call("gn_tcflat_set_precision", self._h.h, self._PRECISIONS[precision])
 
     def set(self, vectors) -> None:
         arr = _as_float2d(vectors, "set")

@@ -16,7 +16,11 @@ def mixture(n, d, nc, nq, seed):
 
 
 @pytest.mark.parametrize("n,d,nq,k,S", [(4096, 128, 128, 10, 40), (50_000, 128, 300, 10, 40),
-                                        (30_001, 64, 77, 5, 32), (20_000, 200, 129, 1, 16)])
+                                        (30_001, 64, 77, 5, 32), (20_000, 200, 129, 1, 16),
+                                        (40_000, 96, 200, 10, 64), (10_000, 128, 130, 10, 48),
+                                        # few rows per cluster: the zero-filled tail of the last
+                                        # 256-row tile would outscore other clusters' rows
+                                        (3000, 64, 77, 10, 40), (3000, 128, 200, 10, 16)])
 def test_tc_shortlist_equals_exact(gn, oracle, n, d, nq, k, S):
     db, q = mixture(n, d, 256, nq, seed=n + d)
     tc = gn.FlatL2TCIndex(shortlist=S)
@@ -30,6 +34,50 @@ def test_tc_shortlist_equals_exact(gn, oracle, n, d, nq, k, S):
     oi, od = oracle.knn_l2sq_f64(db, q[:64], k)
     err = np.abs(dist[:64].astype(np.float64) - np.sqrt(od))
     assert err.max() <= 1e-5 * np.sqrt(od).max()
+
+
+# FP8 E4M3 with per-row scales: the shortlist is approximate, the returned
+# distances are still the exact FP32 distances of the returned rows.  Recall
+# floors sit below the recall of a NumPy emulation of the same quantisation on
+# these inputs (0.985, 0.998, 1.0, 0.99).
+@pytest.mark.parametrize("n,d,nq,k,S,floor", [(50_000, 128, 300, 10, 40, 0.97), (20_000, 200, 129, 5, 32, 0.98),
+                                              (3000, 64, 77, 10, 40, 0.99), (50_000, 128, 300, 10, 56, 0.98)])
+def test_fp8_shortlist_recall_and_exact_distances(gn, oracle, n, d, nq, k, S, floor):
+    db, q = mixture(n, d, 256, nq, seed=n + d)
+    tc = gn.FlatL2TCIndex(shortlist=S, precision="fp8")
+    tc.set(db)
+    idx, dist = tc.search_knn_arrays(q, k)
+    ex = gn.FlatL2Index()
+    ex.set(db)
+    ei, ed = ex.search_knn_arrays(q, k)
+    recall = np.mean([len(set(idx[i]) & set(ei[i])) / k for i in range(nq)])
+    assert recall >= floor, recall
+    assert (idx >= 0).all() and all(len(set(r)) == k for r in idx)
+    assert (np.diff(dist, axis=1) >= 0).all()
+    ref = np.array([[oracle.dist("l2", q[i], db[j]) for j in idx[i]] for i in range(min(nq, 40))], np.float32)
+    assert np.array_equal(dist[:len(ref)].view(np.uint32), ref.view(np.uint32))
+    # rows found by both are reported with identical distances
+    for i in range(nq):
+        got = dict(zip(idx[i].tolist(), dist[i].view(np.uint32).tolist()))
+        want = dict(zip(ei[i].tolist(), ed[i].view(np.uint32).tolist()))
+        assert all(got[r] == want[r] for r in got.keys() & want.keys())
+
+
+def test_precision_switch_after_set(gn):
+    db, q = mixture(20_000, 128, 64, 100, seed=9)
+    tc = gn.FlatL2TCIndex(shortlist=40)
+    tc.set(db)
+    i0, d0 = tc.search_knn_arrays(q, 10)
+    gn._lib.call("gn_tcflat_set_precision", tc._h.h, 1)
+    i1, _ = tc.search_knn_arrays(q, 10)
+    assert np.mean([len(set(i1[i]) & set(i0[i])) / 10 for i in range(len(q))]) > 0.9
+    gn._lib.call("gn_tcflat_set_precision", tc._h.h, 0)
+    i2, d2 = tc.search_knn_arrays(q, 10)
+    assert np.array_equal(i2, i0) and np.array_equal(d2.view(np.uint32), d0.view(np.uint32))
+    with pytest.raises(RuntimeError):
+        gn.FlatL2TCIndex(shortlist=64, precision="fp8")
+    with pytest.raises(ValueError):
+        gn.FlatL2TCIndex(precision="fp4")
 
 
 def test_tc_small_batches_and_tiny_db(gn, oracle):
