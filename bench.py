@@ -428,8 +428,9 @@ def bench_ivf(args, dist, peaks, peak_src):
     e2e = {"value": STEP_QUERIES * args.steps * dist.ws / e2e_s, "unit": "queries/s",
            "h2d_bytes_per_step": int(stepq.nbytes), "d2h_bytes_per_step": int(STEP_QUERIES * K * (8 + 4) + STEP_QUERIES * 8)}
     # kernels per tuned batch: BF16 queries, coarse units, coarse scan, coarse+MLP, planning (one kernel up
-    # to 16,384 (query, list) pairs with 64 probe candidates per query, else five), Qb, units, scan, select
-    launches_per_step = sum(9 if nb_ * 64 <= 16384 else 13 for nb_ in batches)
+    # to 16,384 (query, list) pairs with 64 probe candidates per query, else five), Qb + units (one
+    # kernel), scan, select; the launch list of one step in profiles/ shows the same 8 / 12
+    launches_per_step = sum(8 if nb_ * 64 <= 16384 else 12 for nb_ in batches)
     cent, offs_l, ids = ix.export()
     ix.enable_graphs(0, 0)
     return {"tuned": tuned, "plain": plain, "tc_fixed": tcfix, "tuned_no_graphs": tuned_ng,
