@@ -89,3 +89,29 @@ def test_kmeans_argument_checks(gn):
         gn.kmeans_l2(np.zeros((5, 2), np.float32), 6)
     with pytest.raises(RuntimeError):
         gn.kmeans_l2(np.zeros((5,), np.float32), 2)
+
+
+def test_raster_and_precision_argument_checks_without_gpu(gn):
+    """Argument checks of the raster and the shortlist precision run on the
+    host before any CUDA call."""
+    from pynear_gb300 import _lib
+    lib = _lib.load()
+    s = np.zeros((4, 2), np.float32)
+    xs = np.zeros(3, np.float32)
+    out = np.zeros(9, np.int32)
+    P = _lib.ptr
+    assert lib.gn_voronoi_raster(P(s), 0, P(xs), 3, P(xs), 3, P(out), None, None, 0, None) == _lib.GN_ERR_EMPTY
+    assert lib.gn_voronoi_raster(P(s), 4, P(xs), 0, P(xs), 3, P(out), None, None, 0, None) == _lib.GN_ERR_INVALID
+    assert lib.gn_voronoi_raster(P(s), 4, P(xs), 3, P(xs), 3, None, None, None, 0, None) == _lib.GN_ERR_INVALID
+    rgba = np.zeros(36, np.uint8)
+    assert lib.gn_voronoi_raster(P(s), 4, P(xs), 3, P(xs), 3, None, None, None, 0, P(rgba)) == _lib.GN_ERR_INVALID
+    assert "palette" in _lib.last_error()
+    h = ctypes.c_void_p()
+    assert lib.gn_tcflat_create(56, ctypes.byref(h)) == _lib.GN_OK
+    assert lib.gn_tcflat_set_precision(h, 2) == _lib.GN_ERR_INVALID
+    assert lib.gn_tcflat_set_precision(h, 1) == _lib.GN_OK  # empty index: nothing to convert
+    assert lib.gn_index_destroy(h) == _lib.GN_OK
+    assert lib.gn_tcflat_create(64, ctypes.byref(h)) == _lib.GN_OK
+    assert lib.gn_tcflat_set_precision(h, 1) == _lib.GN_ERR_UNSUPPORTED
+    assert lib.gn_index_destroy(h) == _lib.GN_OK
+    assert lib.gn_tcflat_create(24, ctypes.byref(h)) == _lib.GN_ERR_INVALID
