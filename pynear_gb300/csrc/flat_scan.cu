@@ -18,6 +18,8 @@
 
 namespace gn {
 
+__device__ __forceinline__ uint32_t smem_u32_fs(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
 // ── Hamming scan ───────────────────────────────────────────────────────────
 // db: n rows of w4 uint4 words.  q: nq rows, same layout.
 template <int QW, int R>
@@ -75,30 +77,69 @@ __global__ void __launch_bounds__(128) hamming_scan_kernel(const uint4 *__restri
 
 // ── float scan (L2 / L1 / Linf in the reference's arithmetic order) ───────
 // db: n rows of dp floats (dp % 4 == 0, zero padded past d).
+//
+// Lane l of every warp scores row base + l, the whole row in one thread (the
+// reference's eight-accumulator order needs it).  The rows are not read from
+// global memory lane by lane (32 lines per load instruction, which made the L1
+// the bottleneck): the CTA stages each block of 32 rows x 64 floats into
+// shared memory with coalesced cp.async copies, double-buffered, at a row
+// stride of an odd number of 16-byte words so that the lanes' 16-byte reads
+// of 32 different rows are free of bank conflicts; the four warps (16
+// queries) share each staged block.
+constexpr int FS_KC4 = 16;                         // float4 columns per staged block (64 floats)
+constexpr int FS_TS4 = FS_KC4 + 1;                 // odd row stride in float4
+constexpr size_t FS_TILE_BYTES = 2ull * 32 * FS_TS4 * 16;  // double buffer
+
+__device__ __forceinline__ void cp_async16(void *smem_dst, const void *gsrc, int src_bytes) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(smem_u32_fs(smem_dst)), "l"(gsrc),
+                 "r"(src_bytes)
+                 : "memory");
+}
+
 template <int METRIC, int QW, int R>
 __global__ void __launch_bounds__(128) float_scan_kernel(const float *__restrict__ db, int64_t n, int d, int dp,
                                                          const float *__restrict__ q, int64_t nq, int k,
                                                          int n_slices, int64_t slice_rows, int n_groups,
                                                          uint64_t *__restrict__ part) {
-    extern __shared__ float4 sqf[];  // [WARPS*QW][dp/4]
+    extern __shared__ float4 sqf[];  // [WARPS*QW][dp/4] queries, then [2][32][FS_TS4] row blocks
     const int warps = blockDim.x >> 5;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int unit = blockIdx.x;
     const int slice = unit / n_groups, group = unit % n_groups;
     const int64_t q0 = (int64_t)group * warps * QW;
     const int dp4 = dp >> 2;
+    float4 *tile = sqf + warps * QW * dp4;
 
     const float4 *q4 = reinterpret_cast<const float4 *>(q);
     for (int i = threadIdx.x; i < warps * QW * dp4; i += blockDim.x) {
         int64_t qi = q0 + i / dp4;
         sqf[i] = (qi < nq) ? q4[qi * dp4 + (i % dp4)] : make_float4(0.f, 0.f, 0.f, 0.f);
     }
-    __syncthreads();
 
     const int64_t r0 = (int64_t)slice * slice_rows;
     const int64_t r1 = min(n, r0 + slice_rows);
     const float4 *myq = sqf + warp * QW * dp4;
     const int nb = d >> 3, rem = d & 7;
+    const int tail4 = 2 * nb;  // float4 index of the remainder pair (when rem > 0)
+    const int nchunk = (dp4 + FS_KC4 - 1) / FS_KC4;
+    const int64_t nrb = (r1 - r0 + 31) / 32;
+    const int64_t nstage = nrb * nchunk;
+    const float4 *db4 = reinterpret_cast<const float4 *>(db);
+
+    // stage si = (row block si / nchunk, column block si % nchunk) into buffer buf
+    auto issue = [&](int64_t si, int buf) {
+        const int64_t base = r0 + (si / nchunk) * 32;
+        const int c0 = (int)(si % nchunk) * FS_KC4;
+        const int cw = min(FS_KC4, dp4 - c0);
+        float4 *dst = tile + buf * 32 * FS_TS4;
+        for (int i = threadIdx.x; i < 32 * cw; i += blockDim.x) {
+            const int r = i / cw, c = i - r * cw;
+            const int64_t row = base + r;
+            const bool ok = row < r1;
+            cp_async16(dst + r * FS_TS4 + c, db4 + (ok ? row : r0) * dp4 + c0 + c, ok ? 16 : 0);
+        }
+        asm volatile("cp.async.commit_group;" ::: "memory");
+    };
 
     WarpTopK<R> lists[QW];
     uint64_t thr[QW];
@@ -106,31 +147,49 @@ __global__ void __launch_bounds__(128) float_scan_kernel(const float *__restrict
     for (int j = 0; j < QW; ++j) { lists[j].init(); thr[j] = KEY_EMPTY; }
 
     const float4 zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
-    for (int64_t base = r0; base < r1; base += 32) {
-        const int64_t row = base + lane;
-        const bool valid = row < r1;
-        const float4 *rp = reinterpret_cast<const float4 *>(db) + (valid ? row : r0) * dp4;
-        FAcc<METRIC> acc[QW];
+    FAcc<METRIC> acc[QW];
+    float4 x0t = zero4, x1t = zero4;  // the row's remainder pair
+    if (nstage > 0) issue(0, 0);
+    for (int64_t si = 0; si < nstage; ++si) {
+        if (si + 1 < nstage) {
+            issue(si + 1, (int)((si + 1) & 1));
+            asm volatile("cp.async.wait_group 1;" ::: "memory");
+        } else {
+            asm volatile("cp.async.wait_group 0;" ::: "memory");
+        }
+        __syncthreads();  // stage si (and, the first time, the queries) visible to every warp
+        const int kc = (int)(si % nchunk);
+        const int c0 = kc * FS_KC4;
+        const float4 *rp = tile + (si & 1) * 32 * FS_TS4 + lane * FS_TS4 - c0;  // rp[c] = float4 c of the row
+        if (kc == 0) {
 #pragma unroll
-        for (int j = 0; j < QW; ++j) acc[j].zero();
+            for (int j = 0; j < QW; ++j) acc[j].zero();
+        }
+        const int cb0 = c0 >> 1, cb1 = min(nb, (c0 + FS_KC4) >> 1);  // full blocks of eight in this column block
 #pragma unroll 2
-        for (int c = 0; c < nb; ++c) {
-            float4 x0 = ldg_nc_f4(rp + 2 * c), x1 = ldg_nc_f4(rp + 2 * c + 1);
+        for (int c = cb0; c < cb1; ++c) {
+            const float4 x0 = rp[2 * c], x1 = rp[2 * c + 1];
 #pragma unroll
             for (int j = 0; j < QW; ++j) acc[j].block8(myq[j * dp4 + 2 * c], myq[j * dp4 + 2 * c + 1], x0, x1);
         }
-        float4 x0 = zero4, x1 = zero4;
-        if (rem > 0) x0 = ldg_nc_f4(rp + 2 * nb);
-        if (rem > 4) x1 = ldg_nc_f4(rp + 2 * nb + 1);
-#pragma unroll
-        for (int j = 0; j < QW; ++j) {
-            float4 qa = zero4, qb = zero4;
-            if (rem > 0) qa = myq[j * dp4 + 2 * nb];
-            if (rem > 4) qb = myq[j * dp4 + 2 * nb + 1];
-            float dist = acc[j].finish(rem, qa, qb, x0, x1);
-            uint64_t key = valid ? make_key(__float_as_uint(dist), (uint32_t)row) : KEY_EMPTY;
-            lists[j].offer(key, thr[j], k);
+        if (rem > 0 && tail4 >= c0 && tail4 < c0 + FS_KC4) {
+            x0t = rp[tail4];
+            if (rem > 4) x1t = rp[tail4 + 1];
         }
+        if (kc == nchunk - 1) {
+            const int64_t row = r0 + (si / nchunk) * 32 + lane;
+            const bool valid = row < r1;
+#pragma unroll
+            for (int j = 0; j < QW; ++j) {
+                float4 qa = zero4, qb = zero4;
+                if (rem > 0) qa = myq[j * dp4 + tail4];
+                if (rem > 4) qb = myq[j * dp4 + tail4 + 1];
+                float dist = acc[j].finish(rem, qa, qb, x0t, x1t);
+                uint64_t key = valid ? make_key(__float_as_uint(dist), (uint32_t)row) : KEY_EMPTY;
+                lists[j].offer(key, thr[j], k);
+            }
+        }
+        __syncthreads();  // buffer si & 1 is refilled by the next iteration's issue
     }
 #pragma unroll
     for (int j = 0; j < QW; ++j) {
@@ -299,6 +358,20 @@ static void launch_scan(const FlatScanArgs &a, int n_groups, int threads, size_t
         part, a.n_slices, a.k, a.nq, a.metric == M_HAMMING, a.out_idx, a.out_dist);
 }
 
+// CTAs of the float scan resident per SM for this metric and list size.
+template <int R>
+static int float_scan_occupancy(int metric, int threads, size_t smem) {
+    int nb = 0;
+    if (metric == M_L2)
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, float_scan_kernel<M_L2, 4, R>, threads, smem);
+    else if (metric == M_L1)
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, float_scan_kernel<M_L1, 4, R>, threads, smem);
+    else
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, float_scan_kernel<M_LINF, 4, R>, threads, smem);
+    cudaGetLastError();  // a refused query (e.g. shared memory above the default) reads as 0
+    return nb;
+}
+
 void flat_plan(FlatScanArgs &a) {
     const DevInfo &di = dev_info();
     const int qw = (a.metric == M_HAMMING) ? 8 : 4;
@@ -308,10 +381,33 @@ void flat_plan(FlatScanArgs &a) {
     a.warps = warps;
     a.qw = qw;
     const int64_t n_groups = ceil_div(a.nq, (int64_t)warps * qw);
-    // aim for ~16 CTAs per SM over the launch, slices of at least 512 rows
-    const int64_t target = 16LL * di.num_sms;
-    int64_t slices = std::max<int64_t>(1, ceil_div(target, n_groups));
-    slices = std::min<int64_t>(slices, std::max<int64_t>(1, a.n / 512));
+    const int64_t max_slices = std::max<int64_t>(1, a.n / 512);  // slices of at least 512 rows
+    int64_t slices;
+    if (a.metric == M_HAMMING) {
+        // aim for ~16 CTAs per SM over the launch
+        slices = std::min<int64_t>(std::max<int64_t>(1, ceil_div(16LL * di.num_sms, n_groups)), max_slices);
+    } else {
+        // units of equal cost: pick the slice count (up to about four waves of
+        // resident CTAs) whose last wave is fullest, the fewest slices on a tie
+        const int threads = warps * 32;
+        const size_t smem = (size_t)warps * qw * a.stride4 * 16 + FS_TILE_BYTES;
+        int occ = a.k <= 32 ? float_scan_occupancy<1>(a.metric, threads, smem)
+                  : a.k <= 64 ? float_scan_occupancy<2>(a.metric, threads, smem)
+                  : a.k <= 128 ? float_scan_occupancy<4>(a.metric, threads, smem)
+                               : float_scan_occupancy<8>(a.metric, threads, smem);
+        const int64_t slots = (int64_t)std::max(occ, 1) * di.num_sms;
+        const int64_t hi = std::min<int64_t>(max_slices, std::max<int64_t>(1, ceil_div(4 * slots, n_groups)));
+        slices = 1;
+        double best = -1.0;
+        for (int64_t s = 1; s <= hi; ++s) {
+            const int64_t units = n_groups * s;
+            const double eff = (double)units / (double)(ceil_div(units, slots) * slots);
+            if (eff > best + 1e-9) {
+                best = eff;
+                slices = s;
+            }
+        }
+    }
     a.slice_rows = round_up(ceil_div(a.n, slices), 32);
     a.n_slices = (int)ceil_div(a.n, a.slice_rows);
     a.n_groups = (int)n_groups;
@@ -319,15 +415,18 @@ void flat_plan(FlatScanArgs &a) {
 
 size_t flat_part_bytes(const FlatScanArgs &a) { return (size_t)a.nq * a.n_slices * a.k * sizeof(uint64_t); }
 
+static size_t flat_smem_bytes(const FlatScanArgs &a) {
+    return (size_t)a.warps * a.qw * a.stride4 * 16 + (a.metric == M_HAMMING ? 0 : FS_TILE_BYTES);
+}
+
 int flat_smem_ok(const FlatScanArgs &a) {
-    const size_t smem = (size_t)a.warps * a.qw * a.stride4 * 16;
-    return smem <= (size_t)dev_info().max_smem_optin;
+    return flat_smem_bytes(a) <= (size_t)dev_info().max_smem_optin;
 }
 
 // Launch the warp-select path (k <= 256).  part: flat_part_bytes(a) scratch.
 void flat_launch(const FlatScanArgs &a, uint64_t *part, cudaStream_t st) {
     const int threads = a.warps * 32;
-    const size_t smem = (size_t)a.warps * a.qw * a.stride4 * 16;
+    const size_t smem = flat_smem_bytes(a);
     if (a.k <= 32) launch_scan<1>(a, a.n_groups, threads, smem, part, st);
     else if (a.k <= 64) launch_scan<2>(a, a.n_groups, threads, smem, part, st);
     else if (a.k <= 128) launch_scan<4>(a, a.n_groups, threads, smem, part, st);
