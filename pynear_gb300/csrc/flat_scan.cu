@@ -81,14 +81,30 @@ __global__ void __launch_bounds__(128) hamming_scan_kernel(const uint4 *__restri
 // Lane l of every warp scores row base + l, the whole row in one thread (the
 // reference's eight-accumulator order needs it).  The rows are not read from
 // global memory lane by lane (32 lines per load instruction, which made the L1
-// the bottleneck): the CTA stages each block of 32 rows x 64 floats into
-// shared memory with coalesced cp.async copies, double-buffered, at a row
-// stride of an odd number of 16-byte words so that the lanes' 16-byte reads
-// of 32 different rows are free of bank conflicts; the four warps (16
-// queries) share each staged block.
-constexpr int FS_KC4 = 16;                         // float4 columns per staged block (64 floats)
-constexpr int FS_TS4 = FS_KC4 + 1;                 // odd row stride in float4
-constexpr size_t FS_TILE_BYTES = 2ull * 32 * FS_TS4 * 16;  // double buffer
+// the bottleneck): the CTA stages blocks of rows x 64 floats into shared
+// memory with coalesced cp.async copies, double-buffered, at a row stride of
+// an odd number of 16-byte words so that the lanes' 16-byte reads of 32
+// different rows are free of bank conflicts; the four warps (16 queries)
+// share each staged block.  Rows of at most 64 floats are staged 128 rows at
+// a time (four row blocks per barrier), longer rows 32 rows x 64 floats.
+constexpr int FS_KC4 = 16;  // float4 columns per staged block (64 floats)
+
+struct FsTile {
+    int cw;   // float4 columns staged per row (<= FS_KC4)
+    int ts4;  // row stride in float4 (odd)
+    int rb;   // 32-row blocks per stage
+};
+__host__ __device__ inline FsTile fs_tile(int dp4) {
+    FsTile t;
+    t.cw = dp4 < FS_KC4 ? dp4 : FS_KC4;
+    t.ts4 = t.cw | 1;
+    t.rb = dp4 <= FS_KC4 ? 4 : 1;
+    return t;
+}
+inline size_t fs_tile_bytes(int dp4) {
+    const FsTile t = fs_tile(dp4);
+    return 2ull * t.rb * 32 * t.ts4 * 16;  // double buffer
+}
 
 __device__ __forceinline__ void cp_async16(void *smem_dst, const void *gsrc, int src_bytes) {
     asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(smem_u32_fs(smem_dst)), "l"(gsrc),
@@ -101,7 +117,7 @@ __global__ void __launch_bounds__(128) float_scan_kernel(const float *__restrict
                                                          const float *__restrict__ q, int64_t nq, int k,
                                                          int n_slices, int64_t slice_rows, int n_groups,
                                                          uint64_t *__restrict__ part) {
-    extern __shared__ float4 sqf[];  // [WARPS*QW][dp/4] queries, then [2][32][FS_TS4] row blocks
+    extern __shared__ float4 sqf[];  // [WARPS*QW][dp/4] queries, then [2][rb * 32][ts4] row blocks
     const int warps = blockDim.x >> 5;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int unit = blockIdx.x;
@@ -122,21 +138,23 @@ __global__ void __launch_bounds__(128) float_scan_kernel(const float *__restrict
     const int nb = d >> 3, rem = d & 7;
     const int tail4 = 2 * nb;  // float4 index of the remainder pair (when rem > 0)
     const int nchunk = (dp4 + FS_KC4 - 1) / FS_KC4;
-    const int64_t nrb = (r1 - r0 + 31) / 32;
+    const FsTile ft = fs_tile(dp4);
+    const int srows = ft.rb * 32;  // rows per stage
+    const int64_t nrb = (r1 - r0 + srows - 1) / srows;
     const int64_t nstage = nrb * nchunk;
     const float4 *db4 = reinterpret_cast<const float4 *>(db);
 
-    // stage si = (row block si / nchunk, column block si % nchunk) into buffer buf
+    // stage si = (row group si / nchunk, column block si % nchunk) into buffer buf
     auto issue = [&](int64_t si, int buf) {
-        const int64_t base = r0 + (si / nchunk) * 32;
+        const int64_t base = r0 + (si / nchunk) * srows;
         const int c0 = (int)(si % nchunk) * FS_KC4;
         const int cw = min(FS_KC4, dp4 - c0);
-        float4 *dst = tile + buf * 32 * FS_TS4;
-        for (int i = threadIdx.x; i < 32 * cw; i += blockDim.x) {
+        float4 *dst = tile + buf * srows * ft.ts4;
+        for (int i = threadIdx.x; i < srows * cw; i += blockDim.x) {
             const int r = i / cw, c = i - r * cw;
             const int64_t row = base + r;
             const bool ok = row < r1;
-            cp_async16(dst + r * FS_TS4 + c, db4 + (ok ? row : r0) * dp4 + c0 + c, ok ? 16 : 0);
+            cp_async16(dst + r * ft.ts4 + c, db4 + (ok ? row : r0) * dp4 + c0 + c, ok ? 16 : 0);
         }
         asm volatile("cp.async.commit_group;" ::: "memory");
     };
@@ -160,33 +178,37 @@ __global__ void __launch_bounds__(128) float_scan_kernel(const float *__restrict
         __syncthreads();  // stage si (and, the first time, the queries) visible to every warp
         const int kc = (int)(si % nchunk);
         const int c0 = kc * FS_KC4;
-        const float4 *rp = tile + (si & 1) * 32 * FS_TS4 + lane * FS_TS4 - c0;  // rp[c] = float4 c of the row
-        if (kc == 0) {
-#pragma unroll
-            for (int j = 0; j < QW; ++j) acc[j].zero();
-        }
         const int cb0 = c0 >> 1, cb1 = min(nb, (c0 + FS_KC4) >> 1);  // full blocks of eight in this column block
+        // rb > 1 only when the whole row is one column block (kc == 0 == nchunk - 1)
+        for (int rb = 0; rb < ft.rb; ++rb) {
+            // rp[c] = float4 c of this lane's row
+            const float4 *rp = tile + ((si & 1) * srows + rb * 32 + lane) * ft.ts4 - c0;
+            if (kc == 0) {
+#pragma unroll
+                for (int j = 0; j < QW; ++j) acc[j].zero();
+            }
 #pragma unroll 2
-        for (int c = cb0; c < cb1; ++c) {
-            const float4 x0 = rp[2 * c], x1 = rp[2 * c + 1];
+            for (int c = cb0; c < cb1; ++c) {
+                const float4 x0 = rp[2 * c], x1 = rp[2 * c + 1];
 #pragma unroll
-            for (int j = 0; j < QW; ++j) acc[j].block8(myq[j * dp4 + 2 * c], myq[j * dp4 + 2 * c + 1], x0, x1);
-        }
-        if (rem > 0 && tail4 >= c0 && tail4 < c0 + FS_KC4) {
-            x0t = rp[tail4];
-            if (rem > 4) x1t = rp[tail4 + 1];
-        }
-        if (kc == nchunk - 1) {
-            const int64_t row = r0 + (si / nchunk) * 32 + lane;
-            const bool valid = row < r1;
+                for (int j = 0; j < QW; ++j) acc[j].block8(myq[j * dp4 + 2 * c], myq[j * dp4 + 2 * c + 1], x0, x1);
+            }
+            if (rem > 0 && tail4 >= c0 && tail4 < c0 + FS_KC4) {
+                x0t = rp[tail4];
+                if (rem > 4) x1t = rp[tail4 + 1];
+            }
+            if (kc == nchunk - 1) {
+                const int64_t row = r0 + (si / nchunk) * srows + rb * 32 + lane;
+                const bool valid = row < r1;
 #pragma unroll
-            for (int j = 0; j < QW; ++j) {
-                float4 qa = zero4, qb = zero4;
-                if (rem > 0) qa = myq[j * dp4 + tail4];
-                if (rem > 4) qb = myq[j * dp4 + tail4 + 1];
-                float dist = acc[j].finish(rem, qa, qb, x0t, x1t);
-                uint64_t key = valid ? make_key(__float_as_uint(dist), (uint32_t)row) : KEY_EMPTY;
-                lists[j].offer(key, thr[j], k);
+                for (int j = 0; j < QW; ++j) {
+                    float4 qa = zero4, qb = zero4;
+                    if (rem > 0) qa = myq[j * dp4 + tail4];
+                    if (rem > 4) qb = myq[j * dp4 + tail4 + 1];
+                    float dist = acc[j].finish(rem, qa, qb, x0t, x1t);
+                    uint64_t key = valid ? make_key(__float_as_uint(dist), (uint32_t)row) : KEY_EMPTY;
+                    lists[j].offer(key, thr[j], k);
+                }
             }
         }
         __syncthreads();  // buffer si & 1 is refilled by the next iteration's issue
@@ -390,7 +412,7 @@ void flat_plan(FlatScanArgs &a) {
         // units of equal cost: pick the slice count (up to about four waves of
         // resident CTAs) whose last wave is fullest, the fewest slices on a tie
         const int threads = warps * 32;
-        const size_t smem = (size_t)warps * qw * a.stride4 * 16 + FS_TILE_BYTES;
+        const size_t smem = (size_t)warps * qw * a.stride4 * 16 + fs_tile_bytes(a.stride4);
         int occ = a.k <= 32 ? float_scan_occupancy<1>(a.metric, threads, smem)
                   : a.k <= 64 ? float_scan_occupancy<2>(a.metric, threads, smem)
                   : a.k <= 128 ? float_scan_occupancy<4>(a.metric, threads, smem)
@@ -416,7 +438,7 @@ void flat_plan(FlatScanArgs &a) {
 size_t flat_part_bytes(const FlatScanArgs &a) { return (size_t)a.nq * a.n_slices * a.k * sizeof(uint64_t); }
 
 static size_t flat_smem_bytes(const FlatScanArgs &a) {
-    return (size_t)a.warps * a.qw * a.stride4 * 16 + (a.metric == M_HAMMING ? 0 : FS_TILE_BYTES);
+    return (size_t)a.warps * a.qw * a.stride4 * 16 + (a.metric == M_HAMMING ? 0 : fs_tile_bytes(a.stride4));
 }
 
 int flat_smem_ok(const FlatScanArgs &a) {
