@@ -508,6 +508,10 @@ def bench_flat_l2(args, dist, clocks_mhz):
         torch.cuda.synchronize()
         ms.append(e0.elapsed_time(e1))
     lib.gn_timing_enable(0)
+    torch.cuda.profiler.start()  # profiler region: one exact flat step
+    step()
+    torch.cuda.synchronize()
+    torch.cuda.profiler.stop()
     tot = dist.max(sum(ms) / 1e3)
     import oracle
     oracle.build()
@@ -561,6 +565,11 @@ def bench_voronoi(args, dist, clocks_mhz):
         e1.record(stream)
         torch.cuda.synchronize()
         ms = dist.max(e0.elapsed_time(e1) / steps / 1e3) * 1e3
+        if ns == 4096:
+            torch.cuda.profiler.start()  # profiler region: one 4,096-seed raster
+            r = step()
+            torch.cuda.synchronize()
+            torch.cuda.profiler.stop()
         import oracle
         rows = np.linspace(0, h - 1, 8).astype(np.int64)
         oi, _ = oracle.voronoi_raster(seeds, xs, ys[rows])
