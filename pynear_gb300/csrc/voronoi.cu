@@ -11,12 +11,17 @@
 // thread at stride 256 so every store is coalesced.  Seeds stream through
 // shared memory in tiles of 2048 as (sx, dy²), dy² = (py − sy)² computed once
 // per row, so a pixel–seed pair costs one subtract, one multiply, one add and
-// one compare.  The distance is the flat L2 kernel's arithmetic for d = 2,
+// (seeds taken four at a time) three quarters of a minimum and a quarter of a
+// compare.  The distance is the flat L2 kernel's arithmetic for d = 2,
 // sqrt(rn(rn(dx²) + rn(dy²))) with dx = px − sx, dy = py − sy; the argmin is
 // over that sqrt value with ties to the lower seed index, the same answer the
 // exact flat search1NN gives.  The squared sum prefilters: sqrt is monotone,
 // so a pair can only win if its squared sum is below the current best one,
-// and the sqrt is taken only then (about ln(ns) times per pixel).
+// and the sqrt is taken only then (about ln(ns) times per pixel).  Seeds go
+// four at a time: one compare of the four squared sums' minimum against the
+// best decides (almost always) that none of them can win, and only otherwise
+// are the four offered one by one in seed order, so the branch is taken
+// rarely and costs a quarter of a compare per pair.
 #include <cmath>
 
 #include "index.cuh"
@@ -34,7 +39,7 @@ __global__ void __launch_bounds__(VR_NT) voronoi_kernel(const float2 *__restrict
                                                         float *__restrict__ dist,
                                                         const uchar4 *__restrict__ palette, int npal,
                                                         uchar4 *__restrict__ rgba) {
-    __shared__ float2 sm[VR_TILE];
+    __shared__ __align__(16) float2 sm[VR_TILE];
     const int cbase = blockIdx.x * VR_STRIP + threadIdx.x;
     float px[VR_PX];
 #pragma unroll
@@ -61,21 +66,44 @@ __global__ void __launch_bounds__(VR_NT) voronoi_kernel(const float2 *__restrict
                 sm[j] = make_float2(s.x, __fmul_rn(dy, dy));
             }
             __syncthreads();
-#pragma unroll 4
-            for (int j = 0; j < tn; ++j) {
+            // offer seed `idx` with squared sum s to pixel p (seed order is kept)
+            auto offer = [&](int p, float s, int idx) {
+                if (s < bs[p]) {
+                    const float r = __fsqrt_rn(s);
+                    if (r < br[p]) {  // strictly nearer: equal distances keep the lower index
+                        bs[p] = s;
+                        br[p] = r;
+                        bi[p] = idx;
+                    }
+                }
+            };
+            int j = 0;
+#pragma unroll 2
+            for (; j + 4 <= tn; j += 4) {
+                const float4 e01 = *reinterpret_cast<const float4 *>(sm + j);      // (x, dy²) of seeds j, j + 1
+                const float4 e23 = *reinterpret_cast<const float4 *>(sm + j + 2);  // seeds j + 2, j + 3
+#pragma unroll
+                for (int p = 0; p < VR_PX; ++p) {
+                    const float d0 = __fsub_rn(px[p], e01.x), d1 = __fsub_rn(px[p], e01.z);
+                    const float d2 = __fsub_rn(px[p], e23.x), d3 = __fsub_rn(px[p], e23.z);
+                    const float s0 = __fadd_rn(__fmul_rn(d0, d0), e01.y);
+                    const float s1 = __fadd_rn(__fmul_rn(d1, d1), e01.w);
+                    const float s2 = __fadd_rn(__fmul_rn(d2, d2), e23.y);
+                    const float s3 = __fadd_rn(__fmul_rn(d3, d3), e23.w);
+                    if (fminf(fminf(s0, s1), fminf(s2, s3)) < bs[p]) {
+                        offer(p, s0, t0 + j);
+                        offer(p, s1, t0 + j + 1);
+                        offer(p, s2, t0 + j + 2);
+                        offer(p, s3, t0 + j + 3);
+                    }
+                }
+            }
+            for (; j < tn; ++j) {
                 const float2 e = sm[j];
 #pragma unroll
                 for (int p = 0; p < VR_PX; ++p) {
                     const float dx = __fsub_rn(px[p], e.x);
-                    const float s = __fadd_rn(__fmul_rn(dx, dx), e.y);
-                    if (s < bs[p]) {
-                        const float r = __fsqrt_rn(s);
-                        if (r < br[p]) {  // strictly nearer: equal distances keep the lower index
-                            bs[p] = s;
-                            br[p] = r;
-                            bi[p] = t0 + j;
-                        }
-                    }
+                    offer(p, __fadd_rn(__fmul_rn(dx, dx), e.y), t0 + j);
                 }
             }
         }
