@@ -137,3 +137,24 @@ def test_ivf_tc_engine_same_results_for_every_batch_split(gn):
             np.testing.assert_array_equal(i, ref_i[:n])
             np.testing.assert_array_equal(d, ref_d[:n])
             np.testing.assert_array_equal(cnt, ref_c[:n])
+
+
+def test_tc_shortlist_full_size_1m_x128(gn, oracle):
+    """The tensor-core shortlist configuration at full size: 1M x 128 mixture
+    (1,024 centres, sigma 0.3), 10,000 queries, k 10, shortlist 40: the
+    returned rows equal the exact scan's (indices and distance bits), and the
+    distance error against FP64 on a subset stays within FP32 rounding."""
+    from pynear_gb300 import workloads as W
+
+    db, q, _, _ = W.gaussian_mixture(n=1_000_000, d=128, n_centres=1024, sigma=0.3, zipf_s=0, nq=10_000, seed=11)
+    tc = gn.FlatL2TCIndex(shortlist=40)
+    tc.set(db)
+    idx, dist = tc.search_knn_arrays(q, 10)
+    ex = gn.FlatL2Index()
+    ex.set(db)
+    ei, ed = ex.search_knn_arrays(q, 10)
+    assert np.array_equal(idx, ei)
+    assert np.array_equal(dist.view(np.uint32), ed.view(np.uint32))
+    sub = 200
+    d64 = np.sqrt(((q[:sub, None, :].astype(np.float64) - db[idx[:sub]].astype(np.float64)) ** 2).sum(-1))
+    assert np.abs(dist[:sub] - d64).max() <= 1e-5 * d64.max()
