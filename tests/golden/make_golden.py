@@ -203,7 +203,50 @@ def voronoi():
     save("voronoi.npz", **out)
 
 
-ALL = (float_distances, hamming_kat, vptree_float, vptree_binary, kmeans, ivf_binary, ivf_l2, voronoi)
+def mih():
+    # MIHBinaryIndex (pynear/include/MIH.hpp:58-175) on the shapes of the
+    # reference's tests/test_binary_approx.py:120-170 (random rows, queries a
+    # few flipped bits away) and on clustered rows (bases with up to 6 flipped
+    # bits), where many candidates and distance ties occur.
+    def flip(vec, nf, rng):
+        out = vec.copy()
+        for b in rng.choice(len(out) * 8, size=nf, replace=False):
+            out[b // 8] ^= np.uint8(1 << (b % 8))
+        return out
+
+    def clustered(nbase, per, nb, maxflip, rng):
+        base = rng.integers(0, 256, (nbase, nb), dtype=np.uint8)
+        rows = np.array([flip(base[i], int(rng.integers(0, maxflip + 1)), rng) for i in range(nbase)
+                         for _ in range(per)])
+        return rows[rng.permutation(len(rows))], base
+
+    rng = np.random.default_rng(108)
+    cases = []
+    db = rng.integers(0, 256, (2000, 64), dtype=np.uint8)
+    cases.append(("a", db, np.array([flip(db[i], 5, rng) for i in range(0, 200, 20)]), 8, 10, 8))
+    db, base = clustered(50, 40, 64, 6, rng)
+    cases.append(("b", db, np.array([flip(base[i % 50], 2, rng) for i in range(30)]), 8, 10, 16))
+    db, base = clustered(40, 25, 32, 5, rng)
+    cases.append(("c", db, np.array([flip(base[i % 40], 3, rng) for i in range(20)]), 4, 5, 8))
+    db, base = clustered(30, 30, 16, 4, rng)
+    cases.append(("d", db, np.array([flip(base[i % 30], 1, rng) for i in range(20)]), 4, 8, 12))
+    out = {}
+    for tag, db, q, m, k, radius in cases:
+        ix = _pynear.MIHBinaryIndex(m)
+        ix.set(db)
+        ri, rd = ix.searchKNN(q, k, radius)
+        idx = np.full((len(q), k), -1, np.int64)
+        dist = np.zeros((len(q), k), np.int64)
+        cnt = np.array([len(r) for r in ri], np.int64)
+        for i, (r, d) in enumerate(zip(ri, rd)):
+            idx[i, :len(r)] = r
+            dist[i, :len(d)] = d
+        out.update({f"{tag}_db": db, f"{tag}_q": q, f"{tag}_cfg": np.array([m, k, radius], np.int64),
+                    f"{tag}_idx": idx, f"{tag}_dist": dist, f"{tag}_cnt": cnt})
+    save("mih.npz", **out)
+
+
+ALL = (float_distances, hamming_kat, vptree_float, vptree_binary, kmeans, ivf_binary, ivf_l2, voronoi, mih)
 
 if __name__ == "__main__":
     # optional arguments name the fixtures to (re)generate; none = all

@@ -60,3 +60,21 @@ def test_mih_checks_and_empty_index(gn):
     empty = gn.MIHBinaryIndex()
     empty.set(np.zeros((0, 64), np.uint8))
     assert empty.searchKNN(rng.integers(0, 256, (3, 64), dtype=np.uint8), 5) == ([[], [], []], [[], [], []])
+
+
+def test_mih_matches_reference_fixture(gn):
+    """Against the reference's own MIHBinaryIndex output (tests/golden/mih.npz):
+    same counts and distances, the same rows below each query's k-th distance,
+    and rows at the k-th distance at that distance (the reference orders ties
+    by its hash sets, the library by row)."""
+    from conftest import golden
+    from test_oracle_pin import _mih_agree
+
+    g = golden("mih.npz")
+    for t in "abcd":
+        m, k, radius = (int(v) for v in g[f"{t}_cfg"])
+        db, q = g[f"{t}_db"], g[f"{t}_q"]
+        ix = gn.MIHBinaryIndex(m=m)
+        ix.set(db)
+        idx, dist, cnt = ix.search_knn_arrays(q, k, radius)
+        _mih_agree(idx, dist, cnt, g[f"{t}_idx"], g[f"{t}_dist"], g[f"{t}_cnt"], db, q)

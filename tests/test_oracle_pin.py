@@ -169,3 +169,30 @@ def test_png_writer_and_palette(tmp_path):
     n = int.from_bytes(blob[start - 8:start - 4], "big")
     raw = np.frombuffer(zlib.decompress(blob[start:start + n]), np.uint8).reshape(7, 1 + 5 * 4)
     assert (raw[:, 0] == 0).all() and np.array_equal(raw[:, 1:].reshape(7, 5, 4), img)
+
+
+def _mih_agree(idx, dist, cnt, ref_idx, ref_dist, ref_cnt, db, q):
+    """Same counts and distances; the same rows below each query's k-th
+    distance; at the k-th distance the reference's rows (its hash-set order
+    picks among ties) are at that distance."""
+    assert np.array_equal(cnt, ref_cnt)
+    assert np.array_equal(dist, ref_dist)
+    pc = np.unpackbits(np.arange(256, dtype=np.uint8)[:, None], axis=1).sum(1)
+    for i in range(len(q)):
+        c = cnt[i]
+        if c == 0:
+            continue
+        kth = dist[i, c - 1]
+        below = dist[i, :c] < kth
+        assert set(idx[i, :c][below].tolist()) == set(ref_idx[i, :c][below].tolist())
+        tied = ref_idx[i, :c][~below]
+        assert (pc[np.bitwise_xor(db[tied], q[i])].sum(1) == kth).all()
+
+
+def test_mih_restatement_matches_reference(oracle):
+    g = golden("mih.npz")
+    for t in "abcd":
+        m, k, radius = (int(v) for v in g[f"{t}_cfg"])
+        db, q = g[f"{t}_db"], g[f"{t}_q"]
+        oi, od, oc = oracle.mih_search(db, q, k, m, radius)
+        _mih_agree(oi, od, oc, g[f"{t}_idx"], g[f"{t}_dist"], g[f"{t}_cnt"], db, q)
