@@ -384,13 +384,17 @@ static void launch_scan(const FlatScanArgs &a, int n_groups, int threads, size_t
 template <int R>
 static int float_scan_occupancy(int metric, int threads, size_t smem) {
     int nb = 0;
+    cudaError_t e;
     if (metric == M_L2)
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, float_scan_kernel<M_L2, 4, R>, threads, smem);
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, float_scan_kernel<M_L2, 4, R>, threads, smem);
     else if (metric == M_L1)
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, float_scan_kernel<M_L1, 4, R>, threads, smem);
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, float_scan_kernel<M_L1, 4, R>, threads, smem);
     else
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, float_scan_kernel<M_LINF, 4, R>, threads, smem);
-    cudaGetLastError();  // a refused query (e.g. shared memory above the default) reads as 0
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, float_scan_kernel<M_LINF, 4, R>, threads, smem);
+    if (e != cudaSuccess) {  // a refused query (e.g. shared memory above the default) reads as 0
+        cudaGetLastError();
+        nb = 0;
+    }
     return nb;
 }
 
