@@ -148,6 +148,8 @@ class FlatL2TCIndex:
         self._h = _lib.Handle("gn_tcflat_create", int(shortlist))
         self._n = 0
         self._dim = 0
+        self._host = None
+        self.shortlist = int(shortlist)
         self.precision = precision
         if precision != "bf16":
             _lib.call("gn_tcflat_set_precision", self._h.h, self._PRECISIONS[precision])
@@ -156,6 +158,16 @@ class FlatL2TCIndex:
         arr = _as_float2d(vectors, "set")
         _lib.call("gn_tcflat_set", self._h.h, _lib.ptr(arr), arr.shape[0], arr.shape[1])
         self._n, self._dim = arr.shape
+        self._host = arr.copy()
+
+    # ── pickling: the configuration and the host copy of the rows ──────────
+    def __getstate__(self):
+        return {"shortlist": self.shortlist, "precision": self.precision, "data": self._host}
+
+    def __setstate__(self, state):
+        self.__init__(state["shortlist"], state["precision"])
+        if state.get("data") is not None:
+            self.set(state["data"])
 
     def search_knn_arrays(self, queries, k: int):
         q = _as_float2d(queries, "searchKNN")

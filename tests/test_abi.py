@@ -115,3 +115,12 @@ def test_raster_and_precision_argument_checks_without_gpu(gn):
     assert lib.gn_tcflat_set_precision(h, 1) == _lib.GN_ERR_UNSUPPORTED
     assert lib.gn_index_destroy(h) == _lib.GN_OK
     assert lib.gn_tcflat_create(24, ctypes.byref(h)) == _lib.GN_ERR_INVALID
+
+
+def test_tc_flat_index_pickles_its_configuration(gn):
+    import pickle
+    ix = gn.FlatL2TCIndex(shortlist=56, precision="fp8")
+    st = ix.__getstate__()
+    assert st == {"shortlist": 56, "precision": "fp8", "data": None}
+    ix2 = pickle.loads(pickle.dumps(ix))
+    assert (ix2.shortlist, ix2.precision, ix2._n) == (56, "fp8", 0)
