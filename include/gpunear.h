@@ -79,14 +79,18 @@ int gn_index_size(gn_index *ix, int64_t *n, int64_t *dim);
  * process whose device memory is already owned by another allocator, or a
  * latency-critical loop that cannot take cudaMalloc's synchronisation).  All
  * arguments are device buffers: d_db n rows of nbytes (a multiple of 16)
- * packed bytes, d_queries nq rows of the same width, d_idx / d_dist nq*k int64
- * results (nearest first, ties to the lower row).  The only other memory used
- * is a fixed 16 MB array per device inside the library, so nq * k must be at
- * most 2 Mi (larger requests fail with GN_ERR_INVALID); 1 <= k <= 256.  The
- * first call on a device looks up that array's address (cudaGetSymbolAddress),
- * so make it before any stream capture.  Every call uses the same array: calls
- * that overlap on the GPU (other streams, other threads) race and must be
- * serialised by the caller.  Returns without synchronising `stream`. */
+ * packed bytes, d_queries nq rows of the same width (both 16-byte aligned),
+ * d_idx / d_dist nq*k int64 results (nearest first, ties to the lower row).
+ * The only other memory used is a fixed 16 MB array per device inside the
+ * library, so nq * k must be at most 2 Mi (larger requests fail with
+ * GN_ERR_INVALID); 1 <= k <= 256.  Set-up: the first call on a device loads
+ * the library's scan kernels and that array (the driver loads modules lazily,
+ * and reserves their memory then) and looks up the array's address
+ * (cudaGetSymbolAddress); make that first call (nq = 0 is enough) at set-up
+ * time, with the device current and before any stream capture; later calls
+ * allocate nothing.  Every call uses the same array: calls that overlap on
+ * the GPU (other streams, other threads) race and must be serialised by the
+ * caller.  Returns without synchronising `stream`. */
 int gn_hamming_knn_noalloc(const uint8_t *d_db, int64_t n, int64_t nbytes, const uint8_t *d_queries, int64_t nq,
                            int64_t k, int64_t *d_idx, int64_t *d_dist, void *stream);
 int gn_index_destroy(gn_index *ix);

@@ -3,14 +3,18 @@
 # under the read-only reference checkout, into oracle/_ref/.  Used only to pin the
 # oracle and to generate golden fixtures; nothing shipped links it.
 #
-#   REF=/root/reference bash oracle/build_ref.sh
+#   PYNEAR_REFERENCE=<path of the PyNear 2.2.0 source tree> bash oracle/build_ref.sh
 #
 # Needs g++, OpenMP and pybind11 headers (present in the x86 build container,
 # absent on the GPU host, where this script is a no-op).
 set -euo pipefail
-REF="${REF:-/root/reference}"
+REF="${PYNEAR_REFERENCE:-}"
 HERE="$(cd "$(dirname "$0")" && pwd)"
 OUT="$HERE/_ref"
+if [ -z "$REF" ]; then
+  echo "build_ref: PYNEAR_REFERENCE is not set; skipping" >&2
+  exit 0
+fi
 if [ ! -d "$REF/pynear/include" ]; then
   echo "build_ref: no reference tree at $REF; skipping" >&2
   exit 0

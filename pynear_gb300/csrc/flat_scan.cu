@@ -486,3 +486,22 @@ void flat_large_k_launch(const FlatScanArgs &a, int64_t q_begin, int64_t qc, uin
 }
 
 }  // namespace gn
+
+namespace gn {
+
+// Loads every kernel the Hamming warp-select path can launch (the scan and
+// the merge, for each list width).  With lazy module loading (the default
+// since CUDA 12.2) a kernel's module is loaded, and its device memory
+// allocated, at its first launch; querying the kernel's attributes loads it
+// ahead of that.  Cheap once loaded.
+int flat_preload_hamming() {
+    cudaFuncAttributes fa;
+    const void *fns[] = {(const void *)hamming_scan_kernel<8, 1>, (const void *)hamming_scan_kernel<8, 2>,
+                         (const void *)hamming_scan_kernel<8, 4>, (const void *)hamming_scan_kernel<8, 8>,
+                         (const void *)flat_merge_kernel<1>,      (const void *)flat_merge_kernel<2>,
+                         (const void *)flat_merge_kernel<4>,      (const void *)flat_merge_kernel<8>};
+    for (const void *f : fns) GN_CUDA_TRY(cudaFuncGetAttributes(&fa, f));
+    return GN_OK;
+}
+
+}  // namespace gn

@@ -27,6 +27,7 @@ void flat_plan(FlatScanArgs &a);
 size_t flat_part_bytes(const FlatScanArgs &a);
 int flat_smem_ok(const FlatScanArgs &a);
 void flat_launch(const FlatScanArgs &a, uint64_t *part, cudaStream_t st);
+int flat_preload_hamming();
 int64_t next_pow2(int64_t v);
 void flat_large_k_launch(const FlatScanArgs &a, int64_t q_begin, int64_t qc, uint64_t *keys, uint64_t *sorted,
                          cudaStream_t st);

@@ -8,6 +8,14 @@
 // queries and the results; the only other memory the scan needs (its per-slice
 // partial top-k lists) lives in the fixed array below, which every GPU that
 // loads this library holds until the process exits.
+//
+// Set-up: the library's kernels and this array live in modules that the CUDA
+// driver loads lazily (the default since CUDA 12.2), so the FIRST call on a
+// device loads them, and that load is when the driver reserves the array's
+// 16 MB and the kernels' code.  A caller that must not allocate later makes
+// one call at set-up time (nq = 0 is enough: it loads everything and scans
+// nothing), with that device current and before any stream capture.  After
+// that, calls allocate nothing.
 #include <mutex>
 
 #include "flat_scan.cuh"
@@ -20,25 +28,19 @@ constexpr size_t NOALLOC_SCRATCH_KEYS = (size_t)2 << 20;
 static __device__ __align__(256) uint64_t g_noalloc_scratch[NOALLOC_SCRATCH_KEYS];
 
 // Device address of g_noalloc_scratch on the current device.  The host-side
-// name is only a stand-in, so the address is looked up once per device (with
-// that device current) and cached.
-static int noalloc_scratch(uint64_t **out) {
-    static std::mutex mu;
-    static uint64_t *addr[64] = {nullptr};
-    int dev = 0;
-    GN_CUDA_TRY(cudaGetDevice(&dev));
-    if (dev < 0 || dev >= 64) return fail(GN_ERR_UNSUPPORTED, "device index out of range");
-    std::lock_guard<std::mutex> lk(mu);
-    if (!addr[dev]) {
-        void *p = nullptr;
-        const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e != cudaSuccess || !p) {
-            cudaGetLastError();
-            return fail(GN_ERR_CUDA, std::string("cudaGetSymbolAddress(g_noalloc_scratch): ") + cudaGetErrorString(e));
-        }
-        addr[dev] = reinterpret_cast<uint64_t *>(p);
+// name is only a stand-in, so the address is looked up on every call, with
+// the caller's device current (cheap once the module is loaded; nothing is
+// cached, so a cudaDeviceReset between calls leaves no stale pointer).  The
+// same call loads the scan kernels (see the set-up note above).
+static int noalloc_setup(uint64_t **out) {
+    void *p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || !p) {
+        cudaGetLastError();
+        return fail(GN_ERR_CUDA, std::string("cudaGetSymbolAddress(g_noalloc_scratch): ") + cudaGetErrorString(e));
     }
-    *out = addr[dev];
+    GN_TRY(flat_preload_hamming());
+    *out = reinterpret_cast<uint64_t *>(p);
     return GN_OK;
 }
 
@@ -52,14 +54,19 @@ extern "C" int gn_hamming_knn_noalloc(const uint8_t *d_db, int64_t n, int64_t nb
     if (n <= 0 || n >= 0x7fffffffLL) return fail(GN_ERR_INVALID, "hamming_knn_noalloc: n must be in [1, 2^31-2]");
     if (nbytes <= 0 || nbytes % 16 != 0)
         return fail(GN_ERR_INVALID, "hamming_knn_noalloc: row width must be a positive multiple of 16 bytes");
+    // rows are read as 16-byte vectors: both bases must be 16-byte aligned
+    if (((uintptr_t)d_db | (uintptr_t)d_queries) & 15)
+        return fail(GN_ERR_INVALID, "hamming_knn_noalloc: d_db and d_queries must be 16-byte aligned");
     if (nq < 0) return fail(GN_ERR_INVALID, "hamming_knn_noalloc: negative query count");
     if (k <= 0 || k > FLAT_MAX_K_WARP) return fail(GN_ERR_INVALID, "hamming_knn_noalloc: k must be in [1, 256]");
-    if ((uint64_t)nq * (uint64_t)k > NOALLOC_SCRATCH_KEYS)
-        return fail(GN_ERR_INVALID, "hamming_knn_noalloc: nq * k = " + std::to_string(nq * k) +
-                                        " exceeds the fixed scratch of " + std::to_string(NOALLOC_SCRATCH_KEYS) +
+    // nq * k <= the scratch, tested without forming the (possibly wrapping) product
+    if ((uint64_t)nq > NOALLOC_SCRATCH_KEYS / (uint64_t)k)
+        return fail(GN_ERR_INVALID, "hamming_knn_noalloc: nq * k (nq = " + std::to_string(nq) +
+                                        ", k = " + std::to_string(k) + ") exceeds the fixed scratch of " +
+                                        std::to_string(NOALLOC_SCRATCH_KEYS) +
                                         " keys; split the queries into smaller calls");
     uint64_t *scratch = nullptr;
-    GN_TRY(noalloc_scratch(&scratch));
+    GN_TRY(noalloc_setup(&scratch));
     if (nq == 0) return GN_OK;
     FlatScanArgs a;
     a.metric = M_HAMMING;
@@ -74,6 +81,7 @@ extern "C" int gn_hamming_knn_noalloc(const uint8_t *d_db, int64_t n, int64_t nb
     a.out_dist = d_dist;
     flat_plan(a);
     // fewer database slices when the partial lists would overflow the scratch
+    // (nq * k >= 1 and <= the scratch here, so max_slices >= 1)
     const int64_t max_slices = (int64_t)(NOALLOC_SCRATCH_KEYS / ((uint64_t)nq * (uint64_t)k));
     if (a.n_slices > max_slices) {
         a.slice_rows = round_up(ceil_div(n, max_slices), 32);

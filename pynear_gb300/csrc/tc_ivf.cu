@@ -1,14 +1,14 @@
 // tc_ivf.cu — tensor-core list scan of the float IVF index (store mode).
 //
 // Orientation: the list rows are the MMA's M side (128 rows per tile, one per
-// TMEM lane) and the queries probing the list are the N side, N = 32, 64, 128
-// or 256 (the smallest that holds the work unit's queries), so the MMA work
-// follows the number of queries actually probing the list.  One persistent CTA
-// per SM takes work units (list, chunk of <= 256 queries, chunk of rows) from
-// an atomic counter, largest lists first; warp 0 hands each unit index to the
-// other warps through a 4-slot ring of mbarriers:
+// TMEM lane) and the queries probing the list are the N side, N = 32, 64 or
+// 128 (the smallest that holds the work unit's queries; a unit holds at most
+// 128), so the MMA work follows the number of queries actually probing the
+// list.  One persistent CTA per SM takes work units (list, chunk of <= 128
+// queries, chunk of rows) from an atomic counter, largest lists first; warp 0
+// hands each unit index to the other warps through a 4-slot ring of mbarriers:
 //   warp 0     TMA: per 64-wide K slice, 128 list rows (BF16) and the unit's
-//              N query rows (BF16, bucket order) into a 3-stage ring;
+//              N query rows (BF16, bucket order) into a 6-stage ring;
 //   warp 1     TMEM (4 accumulators x 128 columns) and tcgen05.mma M=128, N, K=16;
 //   warps 2-17 epilogue, two sets of eight: set e takes the tiles whose
 //              accumulator index is odd (e = 1) or even (e = 0), so two tiles
@@ -47,12 +47,12 @@ __device__ __forceinline__ uint32_t ti_ord(float f) {
     return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
 }
 
-__device__ __forceinline__ int ti_nsel(int na) { return na <= 32 ? 32 : na <= 64 ? 64 : na <= 128 ? 128 : 256; }
+__device__ __forceinline__ int ti_nsel(int na) { return na <= 32 ? 32 : na <= 64 ? 64 : 128; }
 
 __global__ void __launch_bounds__(TI_THREADS, 1)
     tc_ivf_kernel(const __grid_constant__ CUtensorMap tmX, const __grid_constant__ CUtensorMap tmQ32,
                   const __grid_constant__ CUtensorMap tmQ64, const __grid_constant__ CUtensorMap tmQ128,
-                  const __grid_constant__ CUtensorMap tmQ256, const TcUnit *__restrict__ units,
+                  const TcUnit *__restrict__ units,
                   const int64_t *__restrict__ n_units_ptr, int K, const float *__restrict__ xnorm,
                   const int64_t *__restrict__ aslot, int seg_mul, float *__restrict__ scores,
                   uint32_t *__restrict__ tmin4, int *__restrict__ err, unsigned long long *__restrict__ next_unit) {
@@ -106,7 +106,7 @@ __global__ void __launch_bounds__(TI_THREADS, 1)
                 if (u < 0) break;
                 const TcUnit un = units[u];
                 const int nsel = ti_nsel(un.na);
-                const CUtensorMap *mq = nsel == 32 ? &tmQ32 : nsel == 64 ? &tmQ64 : nsel == 128 ? &tmQ128 : &tmQ256;
+                const CUtensorMap *mq = nsel == 32 ? &tmQ32 : nsel == 64 ? &tmQ64 : &tmQ128;
                 const uint32_t bytes = TI_A_BYTES + (uint32_t)nsel * TI_BK * 2;
                 const int ntile = (int)((un.r1 - un.r0 + TI_M - 1) / TI_M);
                 for (int t = 0; t < ntile && ok; ++t)
@@ -263,12 +263,11 @@ static int tmap(CUtensorMap *m, const void *base, int64_t rows, int K, int box_r
 int tc_ivf_launch(const TcIvfLaunch &a, cudaStream_t st) {
     if (a.K % TI_BK) return fail(GN_ERR_INVALID, "tensor-core list scan: K must be a multiple of 64");
     if (a.x_rows < TI_M || a.q_rows < 256) return fail(GN_ERR_INVALID, "tensor-core list scan: buffers too small");
-    CUtensorMap mx, m32, m64, m128, m256;
+    CUtensorMap mx, m32, m64, m128;
     GN_TRY(tmap(&mx, a.X, a.x_rows, a.K, TI_M));
     GN_TRY(tmap(&m32, a.Q, a.q_rows, a.K, 32));
     GN_TRY(tmap(&m64, a.Q, a.q_rows, a.K, 64));
     GN_TRY(tmap(&m128, a.Q, a.q_rows, a.K, 128));
-    GN_TRY(tmap(&m256, a.Q, a.q_rows, a.K, 256));
     static bool attr = false;
     if (!attr) {
         GN_CUDA_TRY(cudaFuncSetAttribute(tc_ivf_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TI_SMEM));
@@ -276,7 +275,7 @@ int tc_ivf_launch(const TcIvfLaunch &a, cudaStream_t st) {
     }
     if (!a.next_unit) return fail(GN_ERR_INVALID, "tensor-core list scan: no unit counter");
     GN_CUDA_TRY(cudaMemsetAsync(a.next_unit, 0, sizeof(unsigned long long), st));
-    tc_ivf_kernel<<<a.grid, TI_THREADS, TI_SMEM, st>>>(mx, m32, m64, m128, m256, a.units, a.n_units, a.K, a.xnorm,
+    tc_ivf_kernel<<<a.grid, TI_THREADS, TI_SMEM, st>>>(mx, m32, m64, m128, a.units, a.n_units, a.K, a.xnorm,
                                                         a.aslot, a.seg_mul, a.scores, a.tmin4, a.err, a.next_unit);
     GN_CUDA_TRY(cudaGetLastError());
     return GN_OK;

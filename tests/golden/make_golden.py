@@ -1,10 +1,10 @@
 """Generate the golden fixtures in this folder from the reference itself.
 
-Run in a container that holds the PyNear 2.2.0 source tree (default
-/root/reference, override with REF=...) after ``bash oracle/build_ref.sh`` has
+Run in a container that holds the PyNear 2.2.0 source tree, named by the
+PYNEAR_REFERENCE environment variable, after ``bash oracle/build_ref.sh`` has
 built its extension into oracle/_ref/:
 
-    python tests/golden/make_golden.py
+    PYNEAR_REFERENCE=<source tree> python tests/golden/make_golden.py
 
 Every fixture stores seeded inputs plus the reference's own outputs for them,
 produced through its public Python API (the _pynear extension and the pynear
@@ -20,7 +20,9 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(os.path.dirname(HERE))
-REF = os.environ.get("REF", "/root/reference")
+REF = os.environ.get("PYNEAR_REFERENCE")
+if not REF:
+    sys.exit("make_golden: set PYNEAR_REFERENCE to the PyNear 2.2.0 source tree")
 sys.path.insert(0, os.path.join(REPO, "oracle", "_ref"))
 sys.path.insert(0, REF)
 

@@ -1,6 +1,6 @@
 """Pin the CPU oracle to the reference: committed golden fixtures (made by
 tests/golden/make_golden.py from the reference's own build) and, where the
-reference extension is built here (oracle/_ref), live cross-checks."""
+reference extension is built or installed here, live cross-checks."""
 import os
 import sys
 
@@ -9,15 +9,24 @@ import pytest
 
 from conftest import REPO, golden
 
-REF_DIR = os.path.join(REPO, "oracle", "_ref")
+# the reference extension: built from its sources by oracle/build_ref.sh, or
+# installed with the reference package (pip) under baseline/_ref
+REF_DIRS = [os.path.join(REPO, "oracle", "_ref"), os.path.join(REPO, "baseline", "_ref")]
 
 
 def _ref():
-    if not any(f.startswith("_pynear") for f in os.listdir(REF_DIR)) if os.path.isdir(REF_DIR) else True:
-        pytest.skip("reference extension not built here (oracle/_ref)")
-    sys.path.insert(0, REF_DIR)
-    import _pynear
-    return _pynear
+    for d in REF_DIRS:
+        if not os.path.isdir(d) or not any(f.startswith("_pynear") for f in os.listdir(d)):
+            continue
+        sys.path.insert(0, d)
+        try:
+            import _pynear
+            return _pynear
+        except ImportError:
+            continue
+        finally:
+            sys.path.remove(d)
+    pytest.skip("reference extension not built here (oracle/_ref, baseline/_ref)")
 
 
 def test_float_distances_bitexact(oracle):
