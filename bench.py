@@ -21,9 +21,11 @@ The 3 GB of index data exceed L2, so no flush is needed between steps.
 Also reported: the exact Hamming k-NN workload (1,000,000 x 512-bit uniform
 database, 10,000 queries with 24 flipped bits, k = 10) under "hamming".
 
-``--impl reference`` times the CPU restatement of the reference's IVFFlatL2Index
-search (pynear/forest.py:63-111) on the same index and queries (bounded query
-sample per step, all host threads).
+``--impl reference`` times the reference's own IVFFlatL2Index search
+(pynear/forest.py:63-111, NumPy, run unmodified from the reference package
+installed under baseline/_ref) on the same lists and queries, one process per
+host core, its n_probe calibrated to the same recall target; the oracle's C++
+restatement stands in only where that package is not installed.
 """
 from __future__ import annotations
 
@@ -365,9 +367,9 @@ def bench_ivf(args, dist, peaks, peak_src):
     w = np.zeros(4, np.int64)
     _lib.check(lib.gn_ivfl2_last_work(ix._h.h, w.ctypes.data_as(ctypes.c_void_p)))
     pairs, scored, rows, units = (int(x) for x in w)
-    kpad = ((IVF_D + 63) // 64) * 64
-    # BF16 list rows read once + FP32 scores written + 16-byte minima per 128-row score slot
-    bytes_alg = rows * kpad * 2 + scored * 4 + (scored // 128 + pairs) * 16
+    # algorithmic bytes of the list scan: every distinct probed list's rows read
+    # once, BF16 (d x 2 bytes) plus a 4-byte id per row
+    bytes_alg = rows * (IVF_D * 2 + 4)
     name_v = name.value.decode()
     flops_alg = 2.0 * IVF_D * scored                 # useful MACs x 2
     kms = t.value
@@ -378,7 +380,8 @@ def bench_ivf(args, dist, peaks, peak_src):
                 "unit": "GB/s", "frac": achieved_gbs / hbm_peak, "traffic": profile_traffic(name_v),
                 "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)",
                 "kernel_ms": kms, "batch_queries": nb,
-                "algorithmic_per_launch": {"bytes": int(bytes_alg), "flops": flops_alg, "pairs": pairs,
+                "algorithmic_per_launch": {"bytes": int(bytes_alg), "bytes_rule": "distinct probed list rows x "
+                                           "(2 d + 4)", "flops": flops_alg, "pairs": pairs,
                                            "scored_rows": scored, "distinct_list_rows": rows, "units": units},
                 "tensor": {"achieved_tflops": flops_alg / (kms / 1e3) / 1e12, "peak_tflops": tc_peak,
                            "frac": flops_alg / (kms / 1e3) / 1e12 / tc_peak}}
@@ -454,7 +457,7 @@ def cpu_ivf(index, queries, nprobe, budget_s=10.0):
     labels = np.empty(len(db), np.int32)
     for c in range(len(offs) - 1):
         labels[ids[offs[c]:offs[c + 1]]] = c
-    threads = os.cpu_count() or 1
+    threads = host_cores()
     t0 = time.perf_counter()
     oracle.ivfl2_search(db, cent, labels, queries[:threads], K, nprobe, threads)
     per_q = (time.perf_counter() - t0) / threads
@@ -529,6 +532,80 @@ def bench_flat_l2(args, dist, clocks_mhz):
                          "peak": peak / 1e12, "unit": "TFLOP/s", "frac": flops / (kms / 1e3) / peak,
                          "kernel_ms": kms, "peak_source": f"derived: 128 FP32 FMA/clk/SM x SMs x {mhz:.0f} MHz",
                          "note": "latency-bound at this size (12.8 MB database, 1,000 queries)"}}
+
+
+# ── exact flat L2 at 1M x 128 (larger than L2): HBM-bound small batches ─────
+def bench_flat_l2_hbm(args, dist, peaks, clocks_mhz):
+    """Exact flat L2 in the reference's arithmetic order over a database larger
+    than L2 (1,000,000 x 128 float32, 512 MB): with 8 queries per call the
+    scan streams the database once per call and is bound by HBM (reported in
+    GB/s of database read against the measured copy bandwidth); with 1,024
+    queries per call it is bound by the FP32 pipe (3 flops per element and
+    query).  Indices checked against the oracle on a subset."""
+    import torch
+    import pynear_gb300 as gn
+    from pynear_gb300 import _lib
+
+    rng = np.random.default_rng(17 + dist.rank)
+    db = rng.standard_normal((1_000_000, 128), dtype=np.float32)
+    q = rng.standard_normal((1024, 128), dtype=np.float32)
+    ix = gn.FlatL2Index()
+    ix.set(db)
+    lib = _lib.load()
+    dev = torch.device("cuda", dist.local)
+    stream = torch.cuda.current_stream(dev)
+    d_q = torch.from_numpy(q).to(dev)
+    d_idx = torch.empty((len(q), K), dtype=torch.int64, device=dev)
+    d_dist = torch.empty((len(q), K), dtype=torch.float32, device=dev)
+    hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
+    mhz = clocks_mhz or 2070.0
+    fp32_peak = num_sms() * 128 * 2 * mhz * 1e6
+    out = {"config": {"n": len(db), "d": 128, "k": K, "data": "N(0,1) float32",
+                      "l2": "database (512 MB) exceeds L2; no flush"}}
+    import oracle
+    oracle.build()
+    for nq in (8, 1024):
+        def step():
+            _lib.check(lib.gn_flat_search_knn_device(ix._h.h, vp(d_q), nq, K, vp(d_idx), vp(d_dist),
+                                                     ctypes.c_void_p(stream.cuda_stream)))
+
+        for _ in range(args.warmup):
+            step()
+        torch.cuda.synchronize()
+        steps = max(5, args.steps)
+        kern = []
+        lib.gn_timing_enable(1)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            step()
+            t = ctypes.c_float()
+            _lib.check(lib.gn_timing_last(ctypes.byref(t), None, 0))
+            kern.append(t.value)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        lib.gn_timing_enable(0)
+        ms = dist.max(e0.elapsed_time(e1) / steps / 1e3) * 1e3
+        kms = statistics.median(kern)
+        sub = min(nq, 16)
+        oi, _ = oracle.knn_float("l2", db, q[:sub], K)
+        ok = bool(np.array_equal(d_idx[:sub].cpu().numpy(), oi))
+        gbs = db.nbytes / (kms / 1e3) / 1e9
+        flops = 3.0 * nq * db.size
+        entry = {"value": nq / (ms / 1e3), "unit": "queries/s", "ms_per_call": ms, "kernel_ms": kms,
+                 "indices_equal_oracle": ok, "db_read_gbs": gbs, "fp32_tflops": flops / (kms / 1e3) / 1e12}
+        if nq <= 8:
+            entry["roofline"] = {"bound": "hbm", "kernel": "float_scan_kernel", "achieved": gbs, "peak": hbm_peak,
+                                 "unit": "GB/s", "frac": gbs / hbm_peak,
+                                 "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)",
+                                 "algorithmic_per_launch": {"bytes": int(db.nbytes)}}
+        else:
+            entry["roofline"] = {"bound": "fp32", "kernel": "float_scan_kernel",
+                                 "achieved": flops / (kms / 1e3) / 1e12, "peak": fp32_peak / 1e12, "unit": "TFLOP/s",
+                                 "frac": flops / (kms / 1e3) / fp32_peak,
+                                 "peak_source": f"derived: 128 FP32 FMA/clk/SM x SMs x {mhz:.0f} MHz"}
+        out[f"queries_{nq}"] = entry
+    return out
 
 
 # ── headless Voronoi raster (3840 x 2160 pixels, 64 and 4096 seeds) ─────────
@@ -739,7 +816,7 @@ def cpu_hamming(data, budget_s=5.0):
     import oracle
     oracle.build()
     db, q = data
-    threads = os.cpu_count() or 1
+    threads = host_cores()
     t0 = time.perf_counter()
     oracle.knn_hamming(db, q[:threads], K, threads)
     per_q = (time.perf_counter() - t0) / threads
@@ -752,50 +829,187 @@ def cpu_hamming(data, budget_s=5.0):
 
 
 # ── reference arm ─────────────────────────────────────────────────────────
+# The reference's IVFFlatL2Index search is pure NumPy (pynear/forest.py:63-111,
+# 189-204); the arm runs that code unmodified, loaded from the reference package
+# installed under baseline/_ref (pip install of the reference tree), in one
+# process per host core, each searching its share of the queries.  Its index
+# state (centroids, per-list rows, norms and original ids: what
+# _IVFFlatIndex.set builds, forest.py:36-59) is injected from the same lists
+# the GPU arm searches, so both arms run the same configuration.
+REF_FOREST = os.path.join(REPO, "baseline", "_ref", "pynear", "forest.py")
+_REF_STATE = {}
+
+
+def _ref_worker_init(forest_path, rows_path, offs, ids_path, cent):
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("reference_forest", forest_path)
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    rows = np.load(rows_path, mmap_mode="r")
+    ids = np.load(ids_path, mmap_mode="r")
+    _REF_STATE.update(mod=mod, rows=rows, ids=ids, offs=offs, cent=cent, by_nprobe={}, norms=None)
+
+
+def _ref_index(nprobe):
+    st = _REF_STATE
+    ix = st["by_nprobe"].get(nprobe)
+    if ix is None:
+        ix = st["mod"].IVFFlatL2Index(n_clusters=len(st["cent"]), n_probe=nprobe)
+        offs = st["offs"]
+        data = [np.asarray(st["rows"][offs[c]:offs[c + 1]]) for c in range(len(offs) - 1)]
+        if st["norms"] is None:
+            st["norms"] = [(pts * pts).sum(axis=1) for pts in data]  # as forest.py:57
+        ix._centroids = st["cent"]
+        ix._cluster_data = data
+        ix._cluster_norms = st["norms"]
+        ix._orig_indices = [np.asarray(st["ids"][offs[c]:offs[c + 1]]) for c in range(len(offs) - 1)]
+        st["by_nprobe"][nprobe] = ix
+    return ix
+
+
+def _ref_worker_search(job):
+    queries, nprobe = job
+    idx, dist = _ref_index(nprobe).searchKNN(queries, K)
+    out = np.full((len(queries), K), -1, np.int64)
+    for i, row in enumerate(idx):
+        out[i, :len(row)] = row
+    return out
+
+
+def _exact_topk_cpu(db, q, k, chunk=64):
+    """Exact k nearest rows by squared L2 on the CPU: 4k candidates by the
+    FP32 BLAS form, re-ranked in FP64, ties to the lower row."""
+    xn = np.einsum("ij,ij->i", db, db).astype(np.float64)
+    out = np.empty((len(q), k), np.int64)
+    for i in range(0, len(q), chunk):
+        qc = q[i:i + chunk]
+        dd = xn[None, :] - 2.0 * (qc @ db.T).astype(np.float64)
+        part = np.argpartition(dd, 4 * k, axis=1)[:, :4 * k]
+        for j in range(len(qc)):
+            cand = part[j]
+            e = ((db[cand].astype(np.float64) - qc[j].astype(np.float64)) ** 2).sum(1)
+            out[i + j] = cand[np.lexsort((cand, e))][:k]
+    return out
+
+
+def host_cores() -> int:
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
 def run_reference(args):
-    """CPU restatement of the reference IVF search on the same workload.  The
-    arm uses no GPU: centroids come from the CPU k-means restatement on a
-    20,000-row sample (the reference's full kmeans_l2 at 1M x 512 x 1024 runs for
-    hours on CPU), every row goes to its nearest centroid, and each step times
-    the reference's search algorithm on 256 queries."""
-    import oracle
-    oracle.build()
+    """The reference's own IVF-L2 search (forest.py) on the host cores, on the
+    GPU arm's workload and lists, its n_probe calibrated to Recall@10 >= 0.95."""
+    import multiprocessing as mp
+    import tempfile
+
+    threads = host_cores()
     db, cal, ev, stepq, batches = ivf_data(seed=0)
-    # the reference builds its lists with kmeans_l2 (KMeans.hpp); at 1M x 512 x
-    # 1024 that takes hours on CPU, so centroids come from k-means on a 50,000
-    # row sample and every row is assigned to its nearest centroid
-    rng = np.random.default_rng(0)
-    sample = db[rng.choice(len(db), 20_000, replace=False)]
-    threads = os.cpu_count() or 1
-    _, cent, _ = oracle.kmeans_l2(sample, IVF_NLIST, 5, 42, threads)
-    import torch  # noqa: F401  (CPU only: nearest-centroid assignment via matmul)
-    import torch as T
-    x = T.from_numpy(db)
-    c = T.from_numpy(cent)
-    labels = np.empty(len(db), np.int32)
-    cn = (c * c).sum(1)
-    for i in range(0, len(db), 65536):
-        labels[i:i + 65536] = T.argmin(cn[None, :] - 2 * x[i:i + 65536] @ c.T, dim=1).numpy()
-    nprobe = 28  # the plain GPU arm calibrates to nprobe 28 for Recall@10 >= 0.95 on this workload
+    t0 = time.perf_counter()
+    lists_from = "the library's GPU k-means (the GPU arm's own lists)"
+    try:
+        import __graft_entry__
+        __graft_entry__.build()
+        import torch
+        if not torch.cuda.is_available():
+            raise RuntimeError("no GPU")
+        import pynear_gb300 as gn
+        ix = gn.IVFFlatL2Index(n_clusters=IVF_NLIST, n_probe=1)
+        ix.set(db)
+        cent, offs, ids = ix.export()
+        del ix
+        same_config = True
+    except Exception as e:  # no GPU: lists from the CPU k-means restatement on a sample
+        import oracle
+        oracle.build()
+        lists_from = f"CPU k-means restatement on a 20,000-row sample ({type(e).__name__}: no GPU)"
+        rng = np.random.default_rng(0)
+        sample = db[rng.choice(len(db), 20_000, replace=False)]
+        _, cent, _ = oracle.kmeans_l2(sample, IVF_NLIST, 5, 42, threads)
+        cn = (cent * cent).sum(1)
+        labels = np.concatenate([np.argmin(cn[None, :] - 2 * db[i:i + 65536] @ cent.T, axis=1)
+                                 for i in range(0, len(db), 65536)])
+        order = np.argsort(labels, kind="stable")
+        counts = np.bincount(labels, minlength=len(cent))
+        keep = counts > 0
+        cent = cent[keep]
+        offs = np.concatenate([[0], np.cumsum(counts[keep])]).astype(np.int64)
+        ids = order.astype(np.int64)
+        same_config = False
+    build_s = time.perf_counter() - t0
+    have_ref = os.path.exists(REF_FOREST)
+    gt_cal = _exact_topk_cpu(db, cal[:400], K)
+    gt_ev = _exact_topk_cpu(db, ev[:400], K)
+    if not have_ref:  # the reference package is not installed: the oracle's C++ restatement
+        import oracle
+        oracle.build()
+        labels = np.empty(len(db), np.int32)
+        for c in range(len(offs) - 1):
+            labels[ids[offs[c]:offs[c + 1]]] = c
+
+        def search(q, p):
+            return oracle.ivfl2_search(db, cent, labels, q, K, p, threads)[0]
+        pool = None
+    else:
+        tmp = tempfile.mkdtemp(prefix="ref_ivf_")
+        rows_path, ids_path = os.path.join(tmp, "rows.npy"), os.path.join(tmp, "ids.npy")
+        np.save(rows_path, db[ids])  # rows in list order: each list is a contiguous view
+        np.save(ids_path, ids)
+        for v in ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS", "MKL_NUM_THREADS"):
+            os.environ[v] = "1"  # one BLAS thread per process: the processes use the cores
+        pool = mp.get_context("spawn").Pool(threads, initializer=_ref_worker_init,
+                                            initargs=(REF_FOREST, rows_path, offs, ids_path, cent))
+
+        def search(q, p):
+            parts = np.array_split(q, min(len(q), threads * 2))
+            return np.concatenate(pool.map(_ref_worker_search, [(c, p) for c in parts if len(c)]))
+    # smallest n_probe whose calibration recall reaches CAL_TARGET (the GPU arms' rule)
+    cal_rows, nprobe = [], NPROBES[-1]
+    prev = 0
+    for p in [p for p in NPROBES if p >= 8]:
+        r = recall_at(search(cal[:400], p), gt_cal)
+        cal_rows.append((p, r))
+        if r >= CAL_TARGET:
+            nprobe = p
+            for p2 in range(prev + 1, p):
+                r2 = recall_at(search(cal[:400], p2), gt_cal)
+                cal_rows.append((p2, r2))
+                if r2 >= CAL_TARGET:
+                    nprobe = p2
+                    break
+            break
+        prev = p
+    rec_ev = recall_at(search(ev[:400], nprobe), gt_ev)
+    per_step = threads * 8
     times, n_done = [], 0
     for s in range(args.warmup + args.steps):
-        n = 256
-        sub = stepq[(s * n) % len(stepq):][:n]
+        sub = stepq[(s * per_step) % len(stepq):][:per_step]
         t0 = time.perf_counter()
-        oracle.ivfl2_search(db, cent, labels, sub, K, nprobe, threads)
+        search(sub, nprobe)
         if s >= args.warmup:
             times.append(time.perf_counter() - t0)
             n_done += len(sub)
+    if pool is not None:
+        pool.close()
+        pool.join()
     v = n_done / sum(times)
+    kind = "reference" if have_ref else "port"
+    code = ("the reference's own pynear/forest.py IVFFlatL2Index.searchKNN (NumPy), unmodified, "
+            f"one process per core ({threads})") if have_ref else \
+        f"oracle restatement of forest.py:63-111 ({threads} threads; reference package not installed)"
+    sample = f"{per_step} queries per step from the GPU arm's step queries, nprobe={nprobe}; {code}"
     return {"metric": METRIC, "impl": "reference", "value": v, "unit": "queries/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * statistics.mean(times),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic Gaussian mixture (seeded)",
-            "config": {"workload": "ivf_flat_l2_1Mx512_zipf_nlist1024_k10", "n": IVF_N, "d": IVF_D, "nlist": IVF_NLIST,
-                       "nprobe": nprobe, "k": K},
-            "cpu_baseline": {"value": v, "unit": "queries/s", "cores": threads, "kind": "port",
-                             "sample": f"256 queries per step, nprobe={nprobe} (restatement of forest.py:63-111, "
-                                       f"{threads} threads)"},
+            "data": "synthetic, seeded: Gaussian mixture of 2048 N(0,I) centres, Zipf(1.1) sizes, sigma 0.3",
+            "config": {"workload": "ivf_flat_l2_1Mx512_zipf_nlist1024_k10", "n": IVF_N, "d": IVF_D,
+                       "nlist": IVF_NLIST, "k": K, "nprobe": nprobe, "recall_at_10": rec_ev,
+                       "recall_at_10_calibration": [list(r) for r in cal_rows], "same_lists_as_gpu_arm": same_config,
+                       "lists_from": lists_from, "list_build_s": build_s,
+                       "ground_truth": "exact CPU scan (NumPy), 400 calibration + 400 held-out queries"},
+            "cpu_baseline": {"value": v, "unit": "queries/s", "cores": threads, "kind": kind, "sample": sample},
             "e2e": {"value": v, "unit": "queries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
@@ -823,6 +1037,7 @@ def main():
     ivf = bench_ivf(args, dist, peaks, peak_src)
     ham = bench_hamming(args, dist, peaks, ivf["clocks"].get("sm_mhz"))
     flat_l2 = bench_flat_l2(args, dist, ivf["clocks"].get("sm_mhz"))
+    flat_l2_hbm = bench_flat_l2_hbm(args, dist, peaks, ivf["clocks"].get("sm_mhz"))
     tc_short = bench_tc_shortlist(args, dist, peaks)
     vor = bench_voronoi(args, dist, ivf["clocks"].get("sm_mhz"))
     cb = None
@@ -840,10 +1055,15 @@ def main():
             "config": {"workload": "ivf_flat_l2_1Mx512_zipf_nlist1024_k10", "n": IVF_N, "d": IVF_D,
                        "nlist": IVF_NLIST, "k": K, "queries_per_step": STEP_QUERIES,
                        "batches_per_step": ivf["n_batches"], "batch_sizes": "log-uniform 1..4096",
-                       "tuned": {"engine": "tc (BF16 tcgen05 shortlist 40 + exact FP32 re-rank)",
-                                 "probing": "learned MLP", "prob_threshold": ivf["tuned_threshold"],
-                                 "mean_lists_probed": t["mean_lists_probed"]},
-                       "plain": {"engine": "fp32 CUDA-core scan", "nprobe": ivf["plain_nprobe"]},
+                       "tuned_engine": "tc: learned MLP probing + BF16 tcgen05 shortlist 40 + exact FP32 re-rank",
+                       "plain_engine": "fp32 CUDA-core scan, fixed nprobe",
+                       "recall_at_10_tuned": t["recall_eval"], "recall_at_10_plain": p["recall_eval"],
+                       "recall_at_10_tc_fixed": ivf["tc_fixed"]["recall_eval"],
+                       "recall_eval_queries": N_EVAL, "recall_target": 0.95,
+                       "tuned_over_plain": t["qps"] / p["qps"], "tuned_over_tc_fixed": t["qps"] / ivf["tc_fixed"]["qps"],
+                       "plain_qps": p["qps"], "tc_fixed_qps": ivf["tc_fixed"]["qps"],
+                       "mean_lists_probed": t["mean_lists_probed"], "prob_threshold": ivf["tuned_threshold"],
+                       "plain_nprobe": ivf["plain_nprobe"], "tc_fixed_nprobe": ivf["tuned_nprobe"],
                        "l2": "index data (3 GB) exceeds L2; no flush", "parallelism": f"replicas x{ws}"},
             "recall_at_10": {"tuned": t["recall_eval"], "plain": p["recall_eval"],
                              "calibration": ivf["calibration"]},
@@ -859,7 +1079,8 @@ def main():
                          "chosen": ivf["autotune"]},
             "roofline": ivf["roofline"], "cpu_baseline": cb, "e2e": ivf["e2e"],
             "gpu_launches": ivf["gpu_launches"], "clocks": ivf["clocks"],
-            "build_s": ivf["build_s"], "hamming": ham, "flat_l2_exact": flat_l2, "tc_shortlist": tc_short,
+            "build_s": ivf["build_s"], "hamming": ham, "flat_l2_exact": flat_l2,
+            "flat_l2_exact_1Mx128": flat_l2_hbm, "tc_shortlist": tc_short,
             "voronoi_raster": vor,
         }
         print(json.dumps(line))
