@@ -55,6 +55,14 @@ int gn_device_info(int *num_sms, int *cc_major, int *cc_minor);
 int gn_timing_enable(int on);
 int gn_timing_last(float *ms, char *name, int name_len);
 
+/* Distance between two vectors of d floats (L2: Euclidean, L1, L-inf) or d
+ * bytes (Hamming), host pointers, the result in *out.  Replaces the module
+ * functions dist_l2 / dist_l1 / dist_chebyshev / dist_hamming
+ * (pynear/src/PythonBindings.cpp, DistanceFunctions.hpp:304-448): float values
+ * bit for bit those of dist_*_f_avx2; Hamming the true bit count.  Computed on
+ * the GPU by one small kernel per call (operands in mapped pinned memory). */
+int gn_dist(int32_t metric, const void *a, const void *b, int64_t d, double *out);
+
 /* ── exact flat index ─────────────────────────────────────────────────────
  * Replaces the VP-tree indexes bound in pynear/src/PythonBindings.cpp:344-408
  * (VPTreeNumpyAdapter::set / searchKNN / search1NN, :36-90, and the binary

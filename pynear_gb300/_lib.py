@@ -48,6 +48,7 @@ SIGNATURES = {
     "gn_flat_search_knn_device": [P, P, I64, I64, P, P, P],
     "gn_index_size": [P, P, P],
     "gn_index_destroy": [P],
+    "gn_dist": [I32, P, P, I64, P],
     "gn_hamming_knn_noalloc": [P, I64, I64, P, I64, I64, P, P, P],
     "gn_tcflat_create": [I32, PP],
     "gn_tcflat_set": [P, P, I64, I64],

@@ -16,6 +16,8 @@ float32 L1 / L-inf, int64 Hamming counts.
 """
 from __future__ import annotations
 
+import ctypes
+
 import numpy as np
 
 from . import _lib
@@ -273,18 +275,17 @@ class _VPTreeBinaryEngine(_VPTreeCompat):
 
 # ── single-pair distances (pynear/__init__.py:40-53, PythonBindings.cpp:283-303) ─
 def _pair(metric, binary, a, b):
-    cls = {_lib.METRIC_L2: FlatL2Index, _lib.METRIC_L1: FlatL1Index, _lib.METRIC_LINF: FlatChebyshevIndex,
-           _lib.METRIC_HAMMING: FlatHammingIndex}[metric]
-    ix = cls()
-    if binary:
-        a = np.ascontiguousarray(a, dtype=np.uint8).reshape(1, -1)
-        b = np.ascontiguousarray(b, dtype=np.uint8).reshape(1, -1)
-    else:
-        a = np.ascontiguousarray(a, dtype=np.float32).reshape(1, -1)
-        b = np.ascontiguousarray(b, dtype=np.float32).reshape(1, -1)
-    ix.set(b)
-    _, dist = ix.search_knn_arrays(a, 1)
-    return dist[0, 0].item()
+    """One pair's distance on the GPU (gn_dist: one small kernel per call)."""
+    dt = np.uint8 if binary else np.float32
+    a = np.ascontiguousarray(a, dtype=dt).reshape(-1)
+    b = np.ascontiguousarray(b, dtype=dt).reshape(-1)
+    if a.size != b.size:
+        raise ValueError("invalid data dimension: a and b dimensions must agree.")
+    out = ctypes.c_double()
+    rc = _lib.load().gn_dist(metric, a.ctypes.data, b.ctypes.data, a.size, ctypes.byref(out))
+    if rc:
+        _lib.check(rc, "gn_dist")
+    return out.value
 
 
 def dist_l2(a, b) -> float:
