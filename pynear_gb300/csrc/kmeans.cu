@@ -2,9 +2,12 @@
 //
 // Float (replaces kmeans_l2, pynear/include/KMeans.hpp:25-126):
 //   seeding   k-means++ exactly as the reference: mt19937(seed) draws on the
-//             host, squared dist_l2_f_avx2 distances computed on the device in
-//             the reference's arithmetic order, running double sums on the host
-//             in point order (so small problems pick the very same seeds);
+//             host (taken up front: they do not depend on the data), squared
+//             dist_l2_f_avx2 distances computed on the device in the
+//             reference's arithmetic order, the weighted pick on the device
+//             from double running sums, with the reference's serial double
+//             sums deciding where the two orders could disagree (so the seeds
+//             are the reference's);
 //   assign    argmin_c (|c|^2 - 2 x.c) from an FP32 tile GEMM with a fused
 //             argmin epilogue (first minimum wins, like the reference);
 //   update    per-cluster sums in FP64 (atomic adds), divided once and rounded
@@ -36,6 +39,130 @@ __global__ void kpp_update_kernel(const float *__restrict__ X, int64_t n, int d,
     float v = fdist<M_L2>(c, X + i * dp, d);
     v = __fmul_rn(v, v);
     if (v < min_sq[i]) min_sq[i] = v;
+}
+
+// Per chunk of min_sq (block b: elements [b * chunk, (b + 1) * chunk)), the sum
+// in double, in a fixed order (thread-strided, then a fixed tree).
+__global__ void __launch_bounds__(256) kpp_partial_kernel(const float *__restrict__ min_sq, int64_t n,
+                                                          int64_t chunk, double *__restrict__ part) {
+    __shared__ double red[256];
+    const int64_t b0 = (int64_t)blockIdx.x * chunk, b1 = min(n, b0 + chunk);
+    double s = 0.0;
+    for (int64_t i = b0 + threadIdx.x; i < b1; i += 256) s += (double)min_sq[i];
+    red[threadIdx.x] = s;
+    __syncthreads();
+    for (int o = 128; o > 0; o >>= 1) {
+        if ((int)threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) part[blockIdx.x] = red[0];
+}
+
+// k-means++ draw of centroid ci (one block of 1024 threads), the reference's
+// rule (KMeans.hpp:45-70): r = u * sum(min_sq), the first point whose running
+// sum reaches r (n - 1 if none).  The reference sums in double in point order;
+// here the sums are the chunk partials, scanned, then the chosen chunk's
+// elements.  Both orders' running sums lie within 2 (n - 1) 2^-53 total of the
+// exact ones, so when r is farther than twice that from the chosen point's
+// running sums on both sides, the serial order chooses the same point; if not,
+// thread 0 repeats the reference's serial loop (rare).  The chosen row is
+// copied to C[ci].
+__global__ void __launch_bounds__(1024) kpp_pick_kernel(const float *__restrict__ min_sq, int64_t n, int64_t chunk,
+                                                        int P, const double *__restrict__ part, float u,
+                                                        const float *__restrict__ X, int dp, float *__restrict__ C,
+                                                        int64_t ci) {
+    __shared__ double pre[1024], wsum[32];
+    __shared__ int s_b, s_amb, s_found;
+    __shared__ int64_t s_chosen;
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    // exclusive scan of the chunk sums (P <= 1024)
+    const double v = t < P ? part[t] : 0.0;
+    double inc = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const double y = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o) inc += y;
+    }
+    if (lane == 31) wsum[warp] = inc;
+    if (t == 0) {
+        s_b = P;
+        s_amb = 0;
+        s_found = 0;
+        s_chosen = n - 1;
+    }
+    __syncthreads();
+    double wb = 0.0;
+    for (int w = 0; w < warp; ++w) wb += wsum[w];
+    pre[t] = wb + inc - v;
+    double total = 0.0;
+    for (int w = 0; w < 32; ++w) total += wsum[w];
+    const double r = (double)u * total;
+    const double band = 4.0 * (double)n * 1.1102230246251565e-16 * total;  // 2 x 2 (n - 1) 2^-53 total, rounded up
+    __syncthreads();
+    if (t < P && pre[t] + v >= r) atomicMin(&s_b, t);
+    __syncthreads();
+    const int b = s_b;
+    if (b < P) {
+        // running sums inside chunk b: each thread takes a contiguous piece
+        const int64_t c0 = (int64_t)b * chunk, c1 = min(n, c0 + chunk);
+        const int64_t per = (c1 - c0 + 1023) / 1024;
+        const int64_t p0 = min(c1, c0 + t * per), p1 = min(c1, p0 + per);
+        double ls = 0.0;
+        for (int64_t i = p0; i < p1; ++i) ls += (double)min_sq[i];
+        double li = ls;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const double y = __shfl_up_sync(0xffffffffu, li, o);
+            if (lane >= o) li += y;
+        }
+        if (lane == 31) wsum[warp] = li;
+        __syncthreads();
+        double base = pre[b];
+        for (int w = 0; w < warp; ++w) base += wsum[w];
+        double cum = base + li - ls;  // running sum before this thread's piece
+        int64_t found = -1;
+        double before = 0.0, at = 0.0;
+        for (int64_t i = p0; i < p1; ++i) {
+            const double nx = cum + (double)min_sq[i];
+            if (nx >= r) {
+                found = i;
+                before = cum;
+                at = nx;
+                break;
+            }
+            cum = nx;
+        }
+        // the first piece holding the point: pieces are ordered, so the lowest index wins
+        if (found >= 0) {
+            atomicMin(reinterpret_cast<unsigned long long *>(&s_chosen), (unsigned long long)found);
+            s_found = 1;
+        }
+        __syncthreads();
+        if (found >= 0 && found == s_chosen && !(at - r > band && r - before > band)) s_amb = 1;
+        // the chunk's elements summed in this order fell short of r: the serial rule decides
+        if (t == 0 && !s_found) s_amb = 1;
+    } else if (t == 0) {
+        s_amb = 1;  // r beyond every partial sum: the serial rule decides
+    }
+    __syncthreads();
+    if (s_amb && t == 0) {
+        double tot = 0.0;
+        for (int64_t i = 0; i < n; ++i) tot += (double)min_sq[i];
+        const double rr = (double)u * tot;
+        double c = 0.0;
+        int64_t ch = n - 1;
+        for (int64_t i = 0; i < n; ++i) {
+            c += (double)min_sq[i];
+            if (c >= rr) {
+                ch = i;
+                break;
+            }
+        }
+        s_chosen = ch;
+    }
+    __syncthreads();
+    const int64_t ch = s_chosen;
+    for (int j = t; j < dp; j += 1024) C[ci * dp + j] = X[ch * dp + j];
 }
 
 __global__ void fill_float_kernel(float *p, int64_t n, float v) {
@@ -142,30 +269,27 @@ int kmeans_l2_device(const float *X, int64_t n, int d, int dp, int64_t k, int64_
     std::uniform_real_distribution<float> unif01(0.f, 1.f);
     const size_t row_bytes = (size_t)dp * sizeof(float);
 
-    // k-means++ seeding
+    // k-means++ seeding, all on the device: the reference's draws (the first
+    // point, then one uniform per further centroid) do not depend on the data,
+    // so they are taken from the mt19937 stream up front in the reference's
+    // order; each further centroid is then picked by kpp_pick_kernel
     GN_CUDA_TRY(cudaMemcpyAsync(C, X + pick_point(rng) * dp, row_bytes, cudaMemcpyDeviceToDevice, st));
-    DBuf dmin;
+    std::vector<float> draws((size_t)std::max<int64_t>(k, 1));
+    for (int64_t ci = 1; ci < k; ++ci) draws[(size_t)ci] = unif01(rng);
+    DBuf dmin, dpart;
     GN_TRY(dmin.ensure((size_t)n * sizeof(float)));
-    HBuf hmin;
-    GN_TRY(hmin.ensure((size_t)n * sizeof(float)));
+    const int64_t chunk = std::max<int64_t>(256, ceil_div(n, 1024));
+    const int P = (int)ceil_div(n, chunk);  // <= 1024 chunk sums
+    GN_TRY(dpart.ensure((size_t)P * sizeof(double)));
     const unsigned nb = (unsigned)ceil_div(n, 256);
     fill_float_kernel<<<nb, 256, 0, st>>>(dmin.as<float>(), n, std::numeric_limits<float>::max());
-    float *hm = reinterpret_cast<float *>(hmin.p);
     for (int64_t ci = 1; ci < k; ++ci) {
         kpp_update_kernel<<<nb, 256, 0, st>>>(X, n, d, dp, C + (ci - 1) * dp, dmin.as<float>());
-        GN_CUDA_TRY(cudaMemcpyAsync(hm, dmin.p, (size_t)n * sizeof(float), cudaMemcpyDeviceToHost, st));
-        GN_CUDA_TRY(cudaStreamSynchronize(st));
-        double total = 0.0;
-        for (int64_t i = 0; i < n; ++i) total += (double)hm[i];
-        const double r = (double)unif01(rng) * total;
-        double cum = 0.0;
-        int64_t chosen = n - 1;
-        for (int64_t i = 0; i < n; ++i) {
-            cum += (double)hm[i];
-            if (cum >= r) { chosen = i; break; }
-        }
-        GN_CUDA_TRY(cudaMemcpyAsync(C + ci * dp, X + chosen * dp, row_bytes, cudaMemcpyDeviceToDevice, st));
+        kpp_partial_kernel<<<(unsigned)P, 256, 0, st>>>(dmin.as<float>(), n, chunk, dpart.as<double>());
+        kpp_pick_kernel<<<1, 1024, 0, st>>>(dmin.as<float>(), n, chunk, P, dpart.as<double>(), draws[(size_t)ci], X,
+                                            dp, C, ci);
     }
+    GN_CUDA_TRY(cudaGetLastError());
 
     // Lloyd iterations
     DBuf dsum, dcnt, dchg;

@@ -36,6 +36,21 @@ def test_kmeans_matches_reference_fixture(gn):
         assert inertia(data, labels, cent) <= inertia(data, ref_l, ref_c) * (1 + 1e-4)
 
 
+def test_kmeans_seeds_equal_the_reference_rule(gn, oracle):
+    """k-means++ seeding on the device (draws taken up front, weighted pick
+    from parallel double running sums, the serial rule near a boundary)
+    picks exactly the seeds of the reference's serial loop (KMeans.hpp:45-70),
+    restated by the oracle: max_iter 0 returns the seeds."""
+    rng = np.random.default_rng(8)
+    cases = [(rng.random((1000, 8), dtype=np.float32), 37),
+             (rng.standard_normal((300_001, 16)).astype(np.float32), 256),  # chunks longer than 256 rows
+             (np.repeat(rng.random((50, 12), dtype=np.float32), 40, axis=0), 60)]  # duplicates: zero weights
+    for data, k in cases:
+        _, cent = gn.kmeans_l2(data, k, 0, 42)
+        _, ocent, _ = oracle.kmeans_l2(data, k, 0, 42)
+        assert np.array_equal(cent.view(np.uint32), ocent.view(np.uint32)), (data.shape, k)
+
+
 def test_kmeans_converged_labels_are_nearest_centroid(gn):
     # well separated mixture: Lloyd converges (no label changes) well within
     # max_iter, so the returned labels name each point's nearest centroid
