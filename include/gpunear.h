@@ -187,6 +187,16 @@ int gn_ivfl2_set_tuning(gn_index *ix, const int32_t *table);
 int gn_ivfl2_set_mode(gn_index *ix, int32_t mode, int32_t shortlist);
 /* error word of the last tensor-core launch (nonzero: a bounded wait expired) */
 int gn_ivfl2_error(gn_index *ix, int32_t *err_out);
+/* (gn_ivfl2_error reads the error word after the device has drained and
+ * clears it; gn_ivfl2_search_knn reports it itself as GN_ERR_TIMEOUT.)
+ * Failure drill, for tests (no reference counterpart; it exercises on the GPU
+ * the error path whose host-side analogue is the reference's search exception,
+ * VPTree.hpp:145-147): the next tensor-core list scan of this index issues no
+ * tile copies and bounds its pipeline waits to 200,000 cycles, so they run
+ * out; the launch ends with the error word set and its tensor memory freed,
+ * and the search reports GN_ERR_TIMEOUT.  The drill disarms itself after that
+ * one launch. */
+int gn_ivfl2_failure_drill(gn_index *ix);
 /* Work of the last search, for throughput accounting (no reference
  * counterpart): out[0] (query, probe) pairs, out[1] scored (pair, row)
  * entries, out[2] rows of the distinct lists probed, out[3] tensor-core units. */

@@ -74,6 +74,7 @@ SIGNATURES = {
     "gn_ivfl2_set_n_probe": [P, I32],
     "gn_ivfl2_set_mode": [P, I32, I32],
     "gn_ivfl2_error": [P, P],
+    "gn_ivfl2_failure_drill": [P],
     "gn_ivfl2_last_work": [P, P],
     "gn_ivfl2_info": [P, P, P, P, P],
     "gn_ivfl2_export": [P, P, P, P],

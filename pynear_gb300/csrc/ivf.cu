@@ -893,6 +893,18 @@ void ivf_free(gn_index *ix) {
 
 using namespace gn;
 
+// After a synchronised search: a tensor-core pipeline wait that ran out set
+// the index's error word; report it (and clear it, so the next search runs).
+static int ivfl2_take_error(IvfL2State &S, cudaStream_t st) {
+    if (S.mode != 1 || !S.err.p) return GN_OK;
+    GN_CUDA_TRY(cudaStreamSynchronize(st));
+    int herr = 0;
+    GN_CUDA_TRY(cudaMemcpy(&herr, S.err.p, 4, cudaMemcpyDeviceToHost));
+    if (!herr) return GN_OK;
+    GN_CUDA_TRY(cudaMemset(S.err.p, 0, 4));
+    return fail(GN_ERR_TIMEOUT, "tensor-core IVF search: a pipeline wait timed out; results are invalid");
+}
+
 extern "C" {
 
 int gn_kmeans_l2(const float *data, int64_t n, int64_t d, int64_t k, int64_t max_iter, uint32_t seed,
@@ -1018,8 +1030,10 @@ int gn_ivfl2_search_knn(gn_index *ix, const float *queries, int64_t nq, int64_t 
         return fail(GN_ERR_INVALID, "bad query arguments");
     std::lock_guard<std::mutex> lk(ix->mu);
     if (nq == 0) return GN_OK;
-    if (S.graphs && nq <= S.graphs->max_batch && k == S.graphs->k && !timing_on())
-        return ivfl2_search_graph(ix, queries, true, nq, (int)k, out_idx, out_dist, out_cnt, true, ix->stream);
+    if (S.graphs && nq <= S.graphs->max_batch && k == S.graphs->k && !timing_on() && !S.drill) {
+        GN_TRY(ivfl2_search_graph(ix, queries, true, nq, (int)k, out_idx, out_dist, out_cnt, true, ix->stream));
+        return ivfl2_take_error(S, ix->stream);
+    }
     cudaStream_t st = ix->stream;
     GN_TRY(upload_rows(S.s.q, queries, nq, S.d * 4, S.dp / 4, st));
     GN_TRY(ix->out_idx.ensure((size_t)nq * k * 8));
@@ -1032,7 +1046,7 @@ int gn_ivfl2_search_knn(gn_index *ix, const float *queries, int64_t nq, int64_t 
     GN_CUDA_TRY(cudaMemcpyAsync(out_cnt, ix->part.p, (size_t)nq * 8, cudaMemcpyDeviceToHost, st));
     GN_CUDA_TRY(cudaStreamSynchronize(st));
     GN_CUDA_TRY(cudaGetLastError());
-    return GN_OK;
+    return ivfl2_take_error(S, st);
 }
 
 int gn_ivfl2_set_n_probe(gn_index *ix, int32_t n_probe) {

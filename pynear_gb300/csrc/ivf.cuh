@@ -35,6 +35,7 @@ struct IvfL2State {
     DBuf sel_part, sel_done;     // split selection: partial best-S lists, per-query arrival counters
     DBuf sched;                  // unit counters of the tensor-core scans (coarse, lists)
     DBuf tmin;                   // per (score slot, 32-row quarter): minimum ordered score
+    int drill = 0;               // failure drill armed for the next tensor-core list scan (tests)
     DBuf q16, c16, cunits, cnunits, caslot, cscores;  // tensor-core coarse stage
     // learned probing (prober.cu): attached model and logit threshold
     gn_index *prober = nullptr;

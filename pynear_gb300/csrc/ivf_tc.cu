@@ -893,6 +893,12 @@ int ivfl2_search_tc(gn_index *ix, const float *dQ, int64_t nq, int k, int64_t *d
     a.tmin4 = S.tmin.as<uint32_t>();
     a.err = S.err.as<int>();
     a.next_unit = S.sched.as<unsigned long long>() + 1;
+    if (S.drill) {  // armed failure drill: this launch's waits run out after ~0.1 ms
+        a.drill = 1;
+        a.wait_limit = 200000;
+        S.drill = 0;
+        S.cfg++;
+    }
     a.grid = dev_info().num_sms;
     timing_begin(st, "tc_ivf_kernel");
     GN_TRY(tc_ivf_launch(a, st));
@@ -951,9 +957,26 @@ extern "C" int gn_ivfl2_set_mode(gn_index *ix, int32_t mode, int32_t shortlist) 
 
 extern "C" int gn_ivfl2_error(gn_index *ix, int32_t *err_out) {
     if (!ix || ix->kind != K_IVFL2 || !ix->ivfl2) return fail(GN_ERR_INVALID, "not an IVFFlatL2 index");
+    std::lock_guard<std::mutex> lk(ix->mu);
     int herr = 0;
-    if (ix->ivfl2->err.p) GN_CUDA_TRY(cudaMemcpy(&herr, ix->ivfl2->err.p, 4, cudaMemcpyDeviceToHost));
+    if (ix->ivfl2->err.p) {
+        if (ix->stream) GN_CUDA_TRY(cudaStreamSynchronize(ix->stream));
+        GN_CUDA_TRY(cudaDeviceSynchronize());
+        GN_CUDA_TRY(cudaMemcpy(&herr, ix->ivfl2->err.p, 4, cudaMemcpyDeviceToHost));
+        if (herr) GN_CUDA_TRY(cudaMemset(ix->ivfl2->err.p, 0, 4));  // read and cleared
+    }
     if (err_out) *err_out = herr;
+    return GN_OK;
+}
+
+// Failure drill (tests): the next tensor-core list scan of this index issues
+// no tile copies and bounds its pipeline waits to 200,000 cycles, so they run
+// out: the launch ends early with the error word set and its TMEM freed.
+extern "C" int gn_ivfl2_failure_drill(gn_index *ix) {
+    if (!ix || ix->kind != K_IVFL2 || !ix->ivfl2) return fail(GN_ERR_INVALID, "not an IVFFlatL2 index");
+    std::lock_guard<std::mutex> lk(ix->mu);
+    ix->ivfl2->drill = 1;
+    ix->ivfl2->cfg++;
     return GN_OK;
 }
 

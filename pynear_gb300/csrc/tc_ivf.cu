@@ -55,7 +55,8 @@ __global__ void __launch_bounds__(TI_THREADS, 1)
                   const TcUnit *__restrict__ units,
                   const int64_t *__restrict__ n_units_ptr, int K, const float *__restrict__ xnorm,
                   const int64_t *__restrict__ aslot, int seg_mul, float *__restrict__ scores,
-                  uint32_t *__restrict__ tmin4, int *__restrict__ err, unsigned long long *__restrict__ next_unit) {
+                  uint32_t *__restrict__ tmin4, int *__restrict__ err, unsigned long long *__restrict__ next_unit,
+                  long long wait_limit, int drill) {
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
     uint64_t *bars = reinterpret_cast<uint64_t *>(smem + TI_STAGES * TI_STAGE_BYTES);
@@ -98,7 +99,7 @@ __global__ void __launch_bounds__(TI_THREADS, 1)
             // by orders of magnitude, a static split would leave SMs idle
             for (uint32_t ui = 0; ok; ++ui) {
                 const int r = ui % TI_UR;
-                if (!mbar_wait(uempty + r, ((ui / TI_UR) & 1) ^ 1, verr)) break;
+                if (!mbar_wait(uempty + r, ((ui / TI_UR) & 1) ^ 1, verr, wait_limit)) break;
                 int64_t u = (int64_t)atomicAdd(next_unit, 1ull);
                 if (u >= n_units) u = -1;
                 uring[r] = u;
@@ -113,8 +114,9 @@ __global__ void __launch_bounds__(TI_THREADS, 1)
                     for (int kb = 0; kb < nk; ++kb, ++it) {
                         const int s = it % TI_STAGES;
                         const uint32_t ph = (it / TI_STAGES) & 1;
-                        if (!mbar_wait(empty + s, ph ^ 1, verr)) { ok = false; break; }
+                        if (!mbar_wait(empty + s, ph ^ 1, verr, wait_limit)) { ok = false; break; }
                         uint8_t *sa = smem + s * TI_STAGE_BYTES;
+                        if (drill) continue;  // failure drill: no copies, so the MMA's waits run out
                         mbar_expect_tx(full + s, bytes);
                         tma_load_2d(sa, &tmX, kb * TI_BK, (int)(un.r0 + (int64_t)t * TI_M), full + s);
                         tma_load_2d(sa + TI_A_BYTES, mq, kb * TI_BK, (int)un.a0, full + s);
@@ -127,7 +129,7 @@ __global__ void __launch_bounds__(TI_THREADS, 1)
             bool ok = true;
             for (uint32_t ui = 0; ok; ++ui) {
                 const int r = ui % TI_UR;
-                if (!mbar_wait(ufull + r, (ui / TI_UR) & 1, verr)) break;
+                if (!mbar_wait(ufull + r, (ui / TI_UR) & 1, verr, wait_limit)) break;
                 const int64_t u = uring[r];
                 mbar_arrive(uempty + r);
                 if (u < 0) break;
@@ -138,13 +140,13 @@ __global__ void __launch_bounds__(TI_THREADS, 1)
                 for (int t = 0; t < ntile && ok; ++t, ++tile_it) {
                     const int b = tile_it % TI_NACC;
                     const uint32_t tph = (tile_it / TI_NACC) & 1;
-                    if (!mbar_wait(accempty + b, tph ^ 1, verr)) { ok = false; break; }
+                    if (!mbar_wait(accempty + b, tph ^ 1, verr, wait_limit)) { ok = false; break; }
                     tc_fence_after();
                     const uint32_t dt = tmem + (uint32_t)(b * TI_NMAX);
                     for (int kb = 0; kb < nk; ++kb, ++it) {
                         const int s = it % TI_STAGES;
                         const uint32_t ph = (it / TI_STAGES) & 1;
-                        if (!mbar_wait(full + s, ph, verr)) { ok = false; break; }
+                        if (!mbar_wait(full + s, ph, verr, wait_limit)) { ok = false; break; }
                         tc_fence_after();
                         const uint32_t sa = smem_u32(smem + s * TI_STAGE_BYTES);
                         const uint64_t da = sdesc_sw128(sa), db = sdesc_sw128(sa + TI_A_BYTES);
@@ -165,7 +167,7 @@ __global__ void __launch_bounds__(TI_THREADS, 1)
         bool ok = true;
         for (uint32_t ui = 0; ok; ++ui) {
             const int r = ui % TI_UR;
-            if (!mbar_wait(ufull + r, (ui / TI_UR) & 1, verr)) break;
+            if (!mbar_wait(ufull + r, (ui / TI_UR) & 1, verr, wait_limit)) break;
             const int64_t u = uring[r];
             __syncwarp();
             if (lane == 0) mbar_arrive(uempty + r);
@@ -188,7 +190,7 @@ __global__ void __launch_bounds__(TI_THREADS, 1)
                 const int64_t row = un.r0 + (int64_t)t * TI_M + quad * 32 + lane;
                 const bool rok = row < un.r1;
                 const float xn = rok ? __ldg(xnorm + row) : 0.f;
-                if (!mbar_wait(accfull + b, tph, verr)) { ok = false; break; }
+                if (!mbar_wait(accfull + b, tph, verr, wait_limit)) { ok = false; break; }
                 tc_fence_after();
 #pragma unroll 1
                 for (int cc = 0; grp + 2 * cc < nchunk; ++cc) {
@@ -276,7 +278,8 @@ int tc_ivf_launch(const TcIvfLaunch &a, cudaStream_t st) {
     if (!a.next_unit) return fail(GN_ERR_INVALID, "tensor-core list scan: no unit counter");
     GN_CUDA_TRY(cudaMemsetAsync(a.next_unit, 0, sizeof(unsigned long long), st));
     tc_ivf_kernel<<<a.grid, TI_THREADS, TI_SMEM, st>>>(mx, m32, m64, m128, a.units, a.n_units, a.K, a.xnorm,
-                                                        a.aslot, a.seg_mul, a.scores, a.tmin4, a.err, a.next_unit);
+                                                        a.aslot, a.seg_mul, a.scores, a.tmin4, a.err, a.next_unit,
+                                                        a.wait_limit > 0 ? a.wait_limit : TC_TIMEOUT_CYCLES, a.drill);
     GN_CUDA_TRY(cudaGetLastError());
     return GN_OK;
 }

@@ -20,6 +20,8 @@ struct TcIvfLaunch {
     uint32_t *tmin4 = nullptr;      // optional: per (slot, 32-row quarter) minimum ordered score
     int *err = nullptr;
     unsigned long long *next_unit = nullptr;  // device counter of the dynamic unit schedule (reset per launch)
+    long long wait_limit = 0;       // cycles a pipeline wait may take (0: the default, about 2 s)
+    int drill = 0;                  // failure drill: the producer issues no copies, so the waits run out
     int grid = 0;
 };
 

@@ -39,15 +39,17 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
         : "memory");
     return ok != 0;
 }
-// Bounded wait for the phase with the given parity to complete.
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, volatile int *err) {
+// Bounded wait for the phase with the given parity to complete (at most
+// `limit` cycles; any role that finds the error word set leaves at once).
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, volatile int *err,
+                                          long long limit = TC_TIMEOUT_CYCLES) {
     if (mbar_try_wait(bar, parity)) return true;
     const long long t0 = clock64();
     for (uint32_t i = 1;; ++i) {
         if (mbar_try_wait(bar, parity)) return true;
         if ((i & 255) == 0) {
             if (*err) return false;
-            if (clock64() - t0 > TC_TIMEOUT_CYCLES) {
+            if (clock64() - t0 > limit) {
                 atomicExch((int *)err, 1);
                 return false;
             }
