@@ -196,7 +196,14 @@ static int flat_search_dev(gn_index *ix, const void *d_q, int64_t nq, int64_t k,
         flat_plan(a);
         if (!flat_smem_ok(a)) return fail(GN_ERR_UNSUPPORTED, "dimension too large for the exact flat scan");
         GN_TRY(ix->part.ensure(flat_part_bytes(a)));
-        flat_launch(a, ix->part.as<uint64_t>(), st);
+        if (a.metric != M_HAMMING) {
+            if (!ix->err.p) {
+                GN_TRY(ix->err.ensure(4));
+                GN_CUDA_TRY(cudaMemsetAsync(ix->err.p, 0, 4, st));
+            }
+            a.err = ix->err.as<int>();
+        }
+        GN_TRY(flat_launch(a, ix->part.as<uint64_t>(), st));
     } else {
         // materialise keys for chunks of queries (<= 512 MB of keys per chunk)
         const int64_t p2 = next_pow2(k);
@@ -235,6 +242,14 @@ int gn_flat_search_knn(gn_index *ix, const void *queries, int64_t nq, int64_t k,
     GN_CUDA_TRY(cudaMemcpyAsync(out_idx, ix->out_idx.p, (size_t)nq * k * 8, cudaMemcpyDeviceToHost, st));
     GN_CUDA_TRY(cudaMemcpyAsync(out_dist, ix->out_dist.p, dist_bytes, cudaMemcpyDeviceToHost, st));
     GN_CUDA_TRY(cudaStreamSynchronize(st));
+    if (ix->err.p) {  // a float scan's pipeline wait that ran out (reported once, then cleared)
+        int herr = 0;
+        GN_CUDA_TRY(cudaMemcpy(&herr, ix->err.p, 4, cudaMemcpyDeviceToHost));
+        if (herr) {
+            GN_CUDA_TRY(cudaMemset(ix->err.p, 0, 4));
+            return fail(GN_ERR_TIMEOUT, "flat scan: a pipeline wait timed out; results are invalid");
+        }
+    }
     return GN_OK;
 }
 

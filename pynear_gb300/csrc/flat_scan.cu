@@ -13,12 +13,12 @@
 // per query; here ties go to the lower row index.
 #include "distance.cuh"
 #include "flat_scan.cuh"
+#include "tc_sm100.cuh"
 #include "timing.cuh"
+#include "tmap.cuh"
 #include "topk.cuh"
 
 namespace gn {
-
-__device__ __forceinline__ uint32_t smem_u32_fs(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
 // ── Hamming scan ───────────────────────────────────────────────────────────
 // db: n rows of w4 uint4 words.  q: nq rows, same layout.
@@ -79,57 +79,82 @@ __global__ void __launch_bounds__(128) hamming_scan_kernel(const uint4 *__restri
 // db: n rows of dp floats (dp % 4 == 0, zero padded past d).
 //
 // Lane l of every warp scores row base + l, the whole row in one thread (the
-// reference's eight-accumulator order needs it).  The rows are not read from
-// global memory lane by lane (32 lines per load instruction, which made the L1
-// the bottleneck): the CTA stages blocks of rows x 64 floats into shared
-// memory with coalesced cp.async copies, double-buffered, at a row stride of
-// an odd number of 16-byte words so that the lanes' 16-byte reads of 32
-// different rows are free of bank conflicts; the four warps (16 queries)
-// share each staged block.  Rows of at most 64 floats are staged 128 rows at
-// a time (four row blocks per barrier), longer rows 32 rows x 64 floats.
-constexpr int FS_KC4 = 16;  // float4 columns per staged block (64 floats)
+// reference's eight-accumulator order needs it).  The rows reach shared memory
+// by TMA (cp.async.bulk.tensor) in boxes of 32 floats (128 bytes) x the
+// stage's rows with the 128-byte swizzle, so the 16-byte chunk c of row r sits
+// at chunk c ^ (r & 7) of the row's 128 bytes and the eight lanes of each
+// quarter-warp phase of a 16-byte shared load (eight consecutive rows, same
+// logical chunk) hit eight different bank groups.  Thread 0 keeps FS_STAGES - 1
+// stages in flight ahead of the one consumed (one mbarrier per stage, bounded
+// waits); the warps (16 queries) share each staged row block.
+constexpr int FS_ROWS = 128;  // slices are whole multiples of the short-row stage
+constexpr int FS_BOX = 32;    // floats per box row (128 bytes)
+constexpr int FS_STAGES = 3;
 
-struct FsTile {
-    int cw;   // float4 columns staged per row (<= FS_KC4)
-    int ts4;  // row stride in float4 (odd)
-    int rb;   // 32-row blocks per stage
+// Stage shape: rows of at most 64 floats go 128 rows at a time (four 32-row
+// blocks, the whole row in one stage); longer rows 32 rows at a time, up to
+// 256 floats (8 boxes) per stage and in column chunks beyond that, so that a
+// thread's accumulators (its one row) carry across the chunks of its row.
+// Rows narrower than 32 floats are one box exactly the row's width, without
+// swizzle (16-byte chunk c of row r at r * dp * 4 + 16 c).
+struct FsGeom {
+    int nbx;     // boxes of 32 floats per row
+    int rows;    // rows per stage (128 or 32)
+    int cb;      // boxes per stage
+    int nchunk;  // column chunks per row
+    int bw;      // floats per box row: 32 (swizzled) or the row width (narrow rows)
 };
-__host__ __device__ inline FsTile fs_tile(int dp4) {
-    FsTile t;
-    t.cw = dp4 < FS_KC4 ? dp4 : FS_KC4;
-    t.ts4 = t.cw | 1;
-    t.rb = dp4 <= FS_KC4 ? 4 : 1;
-    return t;
+__host__ __device__ inline FsGeom fs_geom(int dp4) {
+    FsGeom g;
+    g.nbx = (dp4 * 4 + FS_BOX - 1) / FS_BOX;
+    g.bw = dp4 * 4 < FS_BOX ? dp4 * 4 : FS_BOX;
+    if (g.nbx <= 2) {
+        g.rows = 128;
+        g.cb = g.nbx;
+    } else {
+        g.rows = 32;
+        g.cb = g.nbx < 8 ? g.nbx : 8;
+    }
+    g.nchunk = (g.nbx + g.cb - 1) / g.cb;
+    return g;
 }
-inline size_t fs_tile_bytes(int dp4) {
-    const FsTile t = fs_tile(dp4);
-    return 2ull * t.rb * 32 * t.ts4 * 16;  // double buffer
+inline size_t fs_stage_bytes(int dp4) {
+    const FsGeom g = fs_geom(dp4);
+    return (size_t)g.cb * g.rows * g.bw * 4;
 }
-
-__device__ __forceinline__ void cp_async16(void *smem_dst, const void *gsrc, int src_bytes) {
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(smem_u32_fs(smem_dst)), "l"(gsrc),
-                 "r"(src_bytes)
-                 : "memory");
+// queries, then 1024-byte aligned stages, then the stage barriers
+inline size_t fs_smem_bytes(int warps, int qw, int dp4) {
+    return (size_t)warps * qw * dp4 * 16 + 1024 + FS_STAGES * fs_stage_bytes(dp4) + FS_STAGES * 8;
 }
 
 template <int METRIC, int QW, int R>
-__global__ void __launch_bounds__(128) float_scan_kernel(const float *__restrict__ db, int64_t n, int d, int dp,
-                                                         const float *__restrict__ q, int64_t nq, int k,
+__global__ void __launch_bounds__(128) float_scan_kernel(const __grid_constant__ CUtensorMap tm, int64_t n, int d,
+                                                         int dp, const float *__restrict__ q, int64_t nq, int k,
                                                          int n_slices, int64_t slice_rows, int n_groups,
-                                                         uint64_t *__restrict__ part) {
-    extern __shared__ float4 sqf[];  // [WARPS*QW][dp/4] queries, then [2][rb * 32][ts4] row blocks
+                                                         uint64_t *__restrict__ part, int *__restrict__ err) {
+    extern __shared__ float4 sqf[];  // [WARPS*QW][dp/4] queries, then the stage ring
     const int warps = blockDim.x >> 5;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int unit = blockIdx.x;
     const int slice = unit / n_groups, group = unit % n_groups;
     const int64_t q0 = (int64_t)group * warps * QW;
     const int dp4 = dp >> 2;
-    float4 *tile = sqf + warps * QW * dp4;
+    const FsGeom g = fs_geom(dp4);
+    const uint32_t box_bytes = (uint32_t)g.rows * g.bw * 4;
+    const uint32_t stage_bytes = (uint32_t)g.cb * box_bytes;
+    uint8_t *ring = reinterpret_cast<uint8_t *>(
+        (reinterpret_cast<uintptr_t>(sqf + warps * QW * dp4) + 1023) & ~(uintptr_t)1023);
+    uint64_t *full = reinterpret_cast<uint64_t *>(ring + FS_STAGES * stage_bytes);
+    volatile int *verr = err;
 
     const float4 *q4 = reinterpret_cast<const float4 *>(q);
     for (int i = threadIdx.x; i < warps * QW * dp4; i += blockDim.x) {
         int64_t qi = q0 + i / dp4;
         sqf[i] = (qi < nq) ? q4[qi * dp4 + (i % dp4)] : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < FS_STAGES; ++s) mbar_init(full + s, 1);
+        mbar_fence_init();
     }
 
     const int64_t r0 = (int64_t)slice * slice_rows;
@@ -137,26 +162,18 @@ __global__ void __launch_bounds__(128) float_scan_kernel(const float *__restrict
     const float4 *myq = sqf + warp * QW * dp4;
     const int nb = d >> 3, rem = d & 7;
     const int tail4 = 2 * nb;  // float4 index of the remainder pair (when rem > 0)
-    const int nchunk = (dp4 + FS_KC4 - 1) / FS_KC4;
-    const FsTile ft = fs_tile(dp4);
-    const int srows = ft.rb * 32;  // rows per stage
-    const int64_t nrb = (r1 - r0 + srows - 1) / srows;
-    const int64_t nstage = nrb * nchunk;
-    const float4 *db4 = reinterpret_cast<const float4 *>(db);
+    const int64_t nrb = (r1 - r0 + g.rows - 1) / g.rows;
+    const int64_t nstage = nrb * g.nchunk;
 
-    // stage si = (row group si / nchunk, column block si % nchunk) into buffer buf
-    auto issue = [&](int64_t si, int buf) {
-        const int64_t base = r0 + (si / nchunk) * srows;
-        const int c0 = (int)(si % nchunk) * FS_KC4;
-        const int cw = min(FS_KC4, dp4 - c0);
-        float4 *dst = tile + buf * srows * ft.ts4;
-        for (int i = threadIdx.x; i < srows * cw; i += blockDim.x) {
-            const int r = i / cw, c = i - r * cw;
-            const int64_t row = base + r;
-            const bool ok = row < r1;
-            cp_async16(dst + r * ft.ts4 + c, db4 + (ok ? row : r0) * dp4 + c0 + c, ok ? 16 : 0);
-        }
-        asm volatile("cp.async.commit_group;" ::: "memory");
+    // stage si = (row group si / nchunk, column chunk si % nchunk) into ring slot si % FS_STAGES
+    auto issue = [&](int64_t si) {
+        const int slot = (int)(si % FS_STAGES);
+        const int y = (int)(r0 + (si / g.nchunk) * g.rows);
+        const int b0 = (int)(si % g.nchunk) * g.cb;
+        const int nbox = min(g.cb, g.nbx - b0);
+        uint8_t *dst = ring + (size_t)slot * stage_bytes;
+        mbar_expect_tx(full + slot, (uint32_t)nbox * box_bytes);
+        for (int bi = 0; bi < nbox; ++bi) tma_load_2d(dst + bi * box_bytes, &tm, (b0 + bi) * g.bw, y, full + slot);
     };
 
     WarpTopK<R> lists[QW];
@@ -164,41 +181,52 @@ __global__ void __launch_bounds__(128) float_scan_kernel(const float *__restrict
 #pragma unroll
     for (int j = 0; j < QW; ++j) { lists[j].init(); thr[j] = KEY_EMPTY; }
 
+    __syncthreads();  // queries and barriers ready
+    if (threadIdx.x == 0)
+        for (int64_t si = 0; si < min((int64_t)FS_STAGES - 1, nstage); ++si) issue(si);
     const float4 zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
     FAcc<METRIC> acc[QW];
     float4 x0t = zero4, x1t = zero4;  // the row's remainder pair
-    if (nstage > 0) issue(0, 0);
-    for (int64_t si = 0; si < nstage; ++si) {
-        if (si + 1 < nstage) {
-            issue(si + 1, (int)((si + 1) & 1));
-            asm volatile("cp.async.wait_group 1;" ::: "memory");
-        } else {
-            asm volatile("cp.async.wait_group 0;" ::: "memory");
-        }
-        __syncthreads();  // stage si (and, the first time, the queries) visible to every warp
-        const int kc = (int)(si % nchunk);
-        const int c0 = kc * FS_KC4;
-        const int cb0 = c0 >> 1, cb1 = min(nb, (c0 + FS_KC4) >> 1);  // full blocks of eight in this column block
-        // rb > 1 only when the whole row is one column block (kc == 0 == nchunk - 1)
-        for (int rb = 0; rb < ft.rb; ++rb) {
-            // rp[c] = float4 c of this lane's row
-            const float4 *rp = tile + ((si & 1) * srows + rb * 32 + lane) * ft.ts4 - c0;
+    bool ok = true;
+    int64_t si = 0;
+    for (; si < nstage; ++si) {
+        // keep FS_STAGES - 1 stages in flight: slot (si - 1) % FS_STAGES was
+        // released by every thread at the end of the previous iteration
+        if (threadIdx.x == 0 && si + FS_STAGES - 1 < nstage) issue(si + FS_STAGES - 1);
+        const int slot = (int)(si % FS_STAGES);
+        if (!mbar_wait(full + slot, (uint32_t)((si / FS_STAGES) & 1), verr)) ok = false;
+        if (__syncthreads_or(!ok)) break;  // a wait ran out: every thread leaves together
+        const int kc = (int)(si % g.nchunk);
+        const int c0 = kc * g.cb * 8;                      // first float4 of this column chunk
+        const int c1 = min(dp4, c0 + g.cb * 8);
+        const int cb0 = c0 >> 1, cb1 = min(nb, c1 >> 1);  // full blocks of eight in this chunk
+        const uint8_t *st = ring + (size_t)slot * stage_bytes;
+        for (int rb = 0; rb < g.rows / 32; ++rb) {
+            const int rl = rb * 32 + lane;  // row within the stage
+            const int sw = rl & 7;
+            // float4 c of this lane's row (c in [c0, c1)): box (c - c0) / 8, swizzled chunk
+            auto rowf4 = [&](int c) -> float4 {
+                const int cc = c - c0;
+                if (g.bw < FS_BOX) return *reinterpret_cast<const float4 *>(st + rl * (g.bw * 4) + cc * 16);
+                return *reinterpret_cast<const float4 *>(st + (cc >> 3) * box_bytes + rl * 128 +
+                                                         (((cc & 7) ^ sw) << 4));
+            };
             if (kc == 0) {
 #pragma unroll
                 for (int j = 0; j < QW; ++j) acc[j].zero();
             }
 #pragma unroll 2
             for (int c = cb0; c < cb1; ++c) {
-                const float4 x0 = rp[2 * c], x1 = rp[2 * c + 1];
+                const float4 x0 = rowf4(2 * c), x1 = rowf4(2 * c + 1);
 #pragma unroll
                 for (int j = 0; j < QW; ++j) acc[j].block8(myq[j * dp4 + 2 * c], myq[j * dp4 + 2 * c + 1], x0, x1);
             }
-            if (rem > 0 && tail4 >= c0 && tail4 < c0 + FS_KC4) {
-                x0t = rp[tail4];
-                if (rem > 4) x1t = rp[tail4 + 1];
+            if (rem > 0 && tail4 >= c0 && tail4 < c1) {
+                x0t = rowf4(tail4);
+                if (rem > 4) x1t = rowf4(tail4 + 1);
             }
-            if (kc == nchunk - 1) {
-                const int64_t row = r0 + (si / nchunk) * srows + rb * 32 + lane;
+            if (kc == g.nchunk - 1) {
+                const int64_t row = r0 + (si / g.nchunk) * g.rows + rl;
                 const bool valid = row < r1;
 #pragma unroll
                 for (int j = 0; j < QW; ++j) {
@@ -211,7 +239,19 @@ __global__ void __launch_bounds__(128) float_scan_kernel(const float *__restrict
                 }
             }
         }
-        __syncthreads();  // buffer si & 1 is refilled by the next iteration's issue
+        __syncthreads();  // slot si % FS_STAGES is free for the next issue
+    }
+    if (!ok) {
+        // a wait ran out in stage si: let the copies issued for stages si ..
+        // si + FS_STAGES - 1 land (each wait bounded) before the CTA leaves
+        if (threadIdx.x == 0)
+            for (int64_t x = si; x < min(nstage, si + FS_STAGES); ++x) {
+                const int slot = (int)(x % FS_STAGES);
+                const long long t0 = clock64();
+                while (!mbar_try_wait(full + slot, (uint32_t)((x / FS_STAGES) & 1)) && clock64() - t0 < 400000) {
+                }
+            }
+        return;
     }
 #pragma unroll
     for (int j = 0; j < QW; ++j) {
@@ -350,52 +390,64 @@ __global__ void keys_to_output_kernel(const uint64_t *__restrict__ sorted, int64
 
 // ── host-side launchers ───────────────────────────────────────────────────
 template <int R>
-static void launch_scan(const FlatScanArgs &a, int n_groups, int threads, size_t smem, uint64_t *part,
-                        cudaStream_t st) {
+static int launch_scan(const FlatScanArgs &a, int n_groups, int threads, size_t smem, uint64_t *part,
+                       cudaStream_t st) {
     const int units = n_groups * a.n_slices;
-    timing_begin(st, a.metric == M_HAMMING ? "hamming_scan_kernel" : "float_scan_kernel");
     if (a.metric == M_HAMMING) {
+        timing_begin(st, "hamming_scan_kernel");
         auto kern = hamming_scan_kernel<8, R>;
         if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         kern<<<units, threads, smem, st>>>(reinterpret_cast<const uint4 *>(a.db), a.n, a.stride4,
                                            reinterpret_cast<const uint4 *>(a.q), a.nq, a.k, a.n_slices, a.slice_rows,
                                            n_groups, part);
+        timing_end(st);
     } else {
+        if (!a.err) return fail(GN_ERR_INVALID, "float scan: no error word");
+        // the rows as a TMA tensor: n rows x dp floats, boxes of 32 floats x the stage's rows, 128-byte swizzle
+        CUtensorMap tm;
+        const FsGeom fg = fs_geom(a.stride4);
+        GN_TRY(tmap_encode_2d(&tm, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, a.db, (uint64_t)a.stride4 * 4, (uint64_t)a.n,
+                              (uint64_t)a.stride4 * 16, (uint32_t)fg.bw, (uint32_t)fg.rows,
+                              fg.bw == FS_BOX ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_NONE));
+        timing_begin(st, "float_scan_kernel");
 #define GN_FLOAT_SCAN(M)                                                                                          \
     do {                                                                                                          \
         auto kern = float_scan_kernel<M, 4, R>;                                                                   \
         if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); \
-        kern<<<units, threads, smem, st>>>(reinterpret_cast<const float *>(a.db), a.n, a.d, a.stride4 * 4,        \
-                                           reinterpret_cast<const float *>(a.q), a.nq, a.k, a.n_slices,           \
-                                           a.slice_rows, n_groups, part);                                         \
+        kern<<<units, threads, smem, st>>>(tm, a.n, a.d, a.stride4 * 4, reinterpret_cast<const float *>(a.q),     \
+                                           a.nq, a.k, a.n_slices, a.slice_rows, n_groups, part, a.err);           \
     } while (0)
         if (a.metric == M_L2) GN_FLOAT_SCAN(M_L2);
         else if (a.metric == M_L1) GN_FLOAT_SCAN(M_L1);
         else GN_FLOAT_SCAN(M_LINF);
 #undef GN_FLOAT_SCAN
+        timing_end(st);
     }
-    timing_end(st);
     const int qpb = 4;  // queries (warps) per merge block
     flat_merge_kernel<R><<<(unsigned)ceil_div(a.nq, qpb), qpb * 32, 0, st>>>(
         part, a.n_slices, a.k, a.nq, a.metric == M_HAMMING, a.out_idx, a.out_dist);
+    return GN_OK;
 }
 
 // CTAs of the float scan resident per SM for this metric and list size.
-template <int R>
-static int float_scan_occupancy(int metric, int threads, size_t smem) {
+template <int M, int R>
+static int float_scan_occupancy1(int threads, size_t smem) {
     int nb = 0;
-    cudaError_t e;
-    if (metric == M_L2)
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, float_scan_kernel<M_L2, 4, R>, threads, smem);
-    else if (metric == M_L1)
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, float_scan_kernel<M_L1, 4, R>, threads, smem);
-    else
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, float_scan_kernel<M_LINF, 4, R>, threads, smem);
-    if (e != cudaSuccess) {  // a refused query (e.g. shared memory above the default) reads as 0
+    auto kern = float_scan_kernel<M, 4, R>;
+    cudaError_t e = cudaSuccess;
+    if (smem > 48 * 1024) e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, threads, smem);
+    if (e != cudaSuccess) {  // a refused query reads as 0
         cudaGetLastError();
         nb = 0;
     }
     return nb;
+}
+template <int R>
+static int float_scan_occupancy(int metric, int threads, size_t smem) {
+    if (metric == M_L2) return float_scan_occupancy1<M_L2, R>(threads, smem);
+    if (metric == M_L1) return float_scan_occupancy1<M_L1, R>(threads, smem);
+    return float_scan_occupancy1<M_LINF, R>(threads, smem);
 }
 
 void flat_plan(FlatScanArgs &a) {
@@ -416,7 +468,7 @@ void flat_plan(FlatScanArgs &a) {
         // units of equal cost: pick the slice count (up to about four waves of
         // resident CTAs) whose last wave is fullest, the fewest slices on a tie
         const int threads = warps * 32;
-        const size_t smem = (size_t)warps * qw * a.stride4 * 16 + fs_tile_bytes(a.stride4);
+        const size_t smem = fs_smem_bytes(warps, qw, a.stride4);
         int occ = a.k <= 32 ? float_scan_occupancy<1>(a.metric, threads, smem)
                   : a.k <= 64 ? float_scan_occupancy<2>(a.metric, threads, smem)
                   : a.k <= 128 ? float_scan_occupancy<4>(a.metric, threads, smem)
@@ -434,7 +486,8 @@ void flat_plan(FlatScanArgs &a) {
             }
         }
     }
-    a.slice_rows = round_up(ceil_div(a.n, slices), 32);
+    // float scans stage up to 128 rows at a time: whole stages per slice
+    a.slice_rows = round_up(ceil_div(a.n, slices), a.metric == M_HAMMING ? 32 : FS_ROWS);
     a.n_slices = (int)ceil_div(a.n, a.slice_rows);
     a.n_groups = (int)n_groups;
 }
@@ -442,7 +495,7 @@ void flat_plan(FlatScanArgs &a) {
 size_t flat_part_bytes(const FlatScanArgs &a) { return (size_t)a.nq * a.n_slices * a.k * sizeof(uint64_t); }
 
 static size_t flat_smem_bytes(const FlatScanArgs &a) {
-    return (size_t)a.warps * a.qw * a.stride4 * 16 + (a.metric == M_HAMMING ? 0 : fs_tile_bytes(a.stride4));
+    return a.metric == M_HAMMING ? (size_t)a.warps * a.qw * a.stride4 * 16 : fs_smem_bytes(a.warps, a.qw, a.stride4);
 }
 
 int flat_smem_ok(const FlatScanArgs &a) {
@@ -450,13 +503,13 @@ int flat_smem_ok(const FlatScanArgs &a) {
 }
 
 // Launch the warp-select path (k <= 256).  part: flat_part_bytes(a) scratch.
-void flat_launch(const FlatScanArgs &a, uint64_t *part, cudaStream_t st) {
+int flat_launch(const FlatScanArgs &a, uint64_t *part, cudaStream_t st) {
     const int threads = a.warps * 32;
     const size_t smem = flat_smem_bytes(a);
-    if (a.k <= 32) launch_scan<1>(a, a.n_groups, threads, smem, part, st);
-    else if (a.k <= 64) launch_scan<2>(a, a.n_groups, threads, smem, part, st);
-    else if (a.k <= 128) launch_scan<4>(a, a.n_groups, threads, smem, part, st);
-    else launch_scan<8>(a, a.n_groups, threads, smem, part, st);
+    if (a.k <= 32) return launch_scan<1>(a, a.n_groups, threads, smem, part, st);
+    if (a.k <= 64) return launch_scan<2>(a, a.n_groups, threads, smem, part, st);
+    if (a.k <= 128) return launch_scan<4>(a, a.n_groups, threads, smem, part, st);
+    return launch_scan<8>(a, a.n_groups, threads, smem, part, st);
 }
 
 int64_t next_pow2(int64_t v) {

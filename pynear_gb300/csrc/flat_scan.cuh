@@ -16,6 +16,7 @@ struct FlatScanArgs {
     int k = 0;
     int64_t *out_idx = nullptr;  // nq*k
     void *out_dist = nullptr;    // nq*k float32 or int64
+    int *err = nullptr;          // float metrics: device error word of the scan's bounded waits
     // filled by flat_plan
     int warps = 4, qw = 8, n_slices = 1, n_groups = 1;
     int64_t slice_rows = 0;
@@ -26,7 +27,7 @@ constexpr int FLAT_MAX_K_WARP = 256;
 void flat_plan(FlatScanArgs &a);
 size_t flat_part_bytes(const FlatScanArgs &a);
 int flat_smem_ok(const FlatScanArgs &a);
-void flat_launch(const FlatScanArgs &a, uint64_t *part, cudaStream_t st);
+int flat_launch(const FlatScanArgs &a, uint64_t *part, cudaStream_t st);
 int flat_preload_hamming();
 int64_t next_pow2(int64_t v);
 void flat_large_k_launch(const FlatScanArgs &a, int64_t q_begin, int64_t qc, uint64_t *keys, uint64_t *sorted,

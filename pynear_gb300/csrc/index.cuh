@@ -52,6 +52,7 @@ struct gn_index {
     std::mutex mu;
     // per-call scratch (reused across calls)
     gn::DBuf q, part, out_idx, out_dist, keys, sorted;
+    gn::DBuf err;         // float flat scans: error word of their bounded pipeline waits
     // kind-specific state
     gn::IvfL2State *ivfl2 = nullptr;
     gn::IvfBinState *ivfbin = nullptr;

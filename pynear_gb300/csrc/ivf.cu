@@ -851,7 +851,7 @@ static int ivfbin_search_dev(gn_index *ix, const uint8_t *dQ, int64_t nq, int k,
     a.out_dist = T.pdist.p;
     flat_plan(a);
     GN_TRY(T.cpart.ensure(flat_part_bytes(a)));
-    flat_launch(a, T.cpart.as<uint64_t>(), st);
+    GN_TRY(flat_launch(a, T.cpart.as<uint64_t>(), st));
     i64_to_i32_kernel<<<(unsigned)ceil_div(nq * np, 256), 256, 0, st>>>(T.probes64.as<int64_t>(), nq * np,
                                                                       T.probes.as<int32_t>());
     const int64_t slots = nq * max_slots_per_query(S.top_rows, np, S.rc);

@@ -88,7 +88,7 @@ extern "C" int gn_hamming_knn_noalloc(const uint8_t *d_db, int64_t n, int64_t nb
         a.n_slices = (int)ceil_div(n, a.slice_rows);
     }
     if (!flat_smem_ok(a)) return fail(GN_ERR_UNSUPPORTED, "hamming_knn_noalloc: rows too wide for the scan");
-    flat_launch(a, scratch, (cudaStream_t)stream);
+    GN_TRY(flat_launch(a, scratch, (cudaStream_t)stream));
     GN_CUDA_TRY(cudaGetLastError());
     return GN_OK;
 }

@@ -27,6 +27,7 @@
 #include "index.cuh"
 #include "tc_ivf.cuh"
 #include "tc_sm100.cuh"
+#include "tmap.cuh"
 
 namespace gn {
 
@@ -231,35 +232,10 @@ __global__ void __launch_bounds__(TI_THREADS, 1)
     if (warp == 1) tmem_dealloc(tmem, 512);
 }
 
-typedef CUresult (*EncodeTiledFnI)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
-                                   const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
-                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
-
-static EncodeTiledFnI encode_fn() {
-    static EncodeTiledFnI fn = nullptr;
-    if (!fn) {
-        void *p = nullptr;
-        cudaDriverEntryPointQueryResult q;
-        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
-                cudaSuccess &&
-            q == cudaDriverEntryPointSuccess)
-            fn = reinterpret_cast<EncodeTiledFnI>(p);
-    }
-    return fn;
-}
-
+// K-major BF16 rows, boxes of 64 elements (one 128-byte swizzle row) x box_rows rows.
 static int tmap(CUtensorMap *m, const void *base, int64_t rows, int K, int box_rows) {
-    EncodeTiledFnI enc = encode_fn();
-    if (!enc) return fail(GN_ERR_CUDA, "cuTensorMapEncodeTiled is unavailable");
-    cuuint64_t dims[2] = {(cuuint64_t)K, (cuuint64_t)rows};
-    cuuint64_t strides[1] = {(cuuint64_t)K * 2};
-    cuuint32_t box[2] = {(cuuint32_t)TI_BK, (cuuint32_t)box_rows};
-    cuuint32_t estr[2] = {1, 1};
-    CUresult r = enc(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void *>(base), dims, strides, box, estr,
-                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-    if (r != CUDA_SUCCESS) return fail(GN_ERR_CUDA, "cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
-    return GN_OK;
+    return tmap_encode_2d(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, base, (uint64_t)K, (uint64_t)rows, (uint64_t)K * 2,
+                          TI_BK, (uint32_t)box_rows, CU_TENSOR_MAP_SWIZZLE_128B);
 }
 
 int tc_ivf_launch(const TcIvfLaunch &a, cudaStream_t st) {

@@ -37,6 +37,7 @@
 #include "kmeans.cuh"
 #include "tc_scan.cuh"
 #include "tc_sm100.cuh"
+#include "tmap.cuh"
 #include "timing.cuh"
 #include "topk.cuh"
 
@@ -401,41 +402,12 @@ __global__ void __launch_bounds__(tc_threads(S), 1)
 }
 
 // ── host: tensor maps and launch ──────────────────────────────────────────
-// cuTensorMapEncodeTiled, resolved through the runtime so that the library has
-// no link-time dependency on the driver library.
-typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
-                                  const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
-                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
-
-static EncodeTiledFn encode_tiled() {
-    static EncodeTiledFn fn = nullptr;
-    if (!fn) {
-        void *p = nullptr;
-        cudaDriverEntryPointQueryResult q;
-        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
-                cudaSuccess &&
-            q == cudaDriverEntryPointSuccess)
-            fn = reinterpret_cast<EncodeTiledFn>(p);
-    }
-    return fn;
-}
-
 // K-major operand rows of K elements (BF16, or FP8 stored as bytes), boxes of
 // 128 bytes of K by box_rows rows, 128-byte swizzle.
 static int make_tmap_rows(CUtensorMap *map, const void *base, int64_t rows, int64_t K, int box_rows, bool f8) {
-    EncodeTiledFn cuTensorMapEncodeTiled = encode_tiled();
-    if (!cuTensorMapEncodeTiled) return fail(GN_ERR_CUDA, "cuTensorMapEncodeTiled is unavailable");
-    cuuint64_t dims[2] = {(cuuint64_t)K, (cuuint64_t)rows};
-    cuuint64_t strides[1] = {(cuuint64_t)K * (f8 ? 1 : 2)};
-    cuuint32_t box[2] = {(cuuint32_t)(f8 ? TC_BK8 : TC_BK), (cuuint32_t)box_rows};
-    cuuint32_t estr[2] = {1, 1};
-    CUresult r = cuTensorMapEncodeTiled(map, f8 ? CU_TENSOR_MAP_DATA_TYPE_UINT8 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2,
-                                        const_cast<void *>(base), dims,
-                                        strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
-                                        CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                                        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-    if (r != CUDA_SUCCESS) return fail(GN_ERR_CUDA, "cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
-    return GN_OK;
+    return tmap_encode_2d(map, f8 ? CU_TENSOR_MAP_DATA_TYPE_UINT8 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, base,
+                          (uint64_t)K, (uint64_t)rows, (uint64_t)K * (f8 ? 1 : 2), f8 ? TC_BK8 : TC_BK,
+                          (uint32_t)box_rows, CU_TENSOR_MAP_SWIZZLE_128B);
 }
 
 int tc_topk_launch(const TcLaunch &a, cudaStream_t st) {
