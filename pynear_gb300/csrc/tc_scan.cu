@@ -21,9 +21,11 @@
 //              first reduced to its minimum, which is compared with the
 //              threshold (the heap's root, and the other half's root): most
 //              blocks end there, the rest are filtered score by score.
-// At the end of a unit each query's S keys go to its partial slot; the re-rank
-// kernel merges a query's slots, keeps the S best by BF16 score, recomputes
-// their distances exactly in FP32 and returns the k nearest.
+// At the end of a unit each query's S keys go to its partial slot, and a full
+// list's S-th best score is published as the query's bound (atomicMin), below
+// which later units of the query filter from their start; the re-rank kernel
+// merges a query's slots, keeps the S best by BF16 score, recomputes their
+// distances exactly in FP32 and returns the k nearest.
 #include <cuda_bf16.h>
 #include <cuda_fp8.h>
 
@@ -95,7 +97,8 @@ __global__ void __launch_bounds__(tc_threads(S), 1)
                    const int64_t *__restrict__ cta_off, int K, int kblk,
                    const float *__restrict__ bnorm, const float *__restrict__ ascale,
                    const float *__restrict__ bscale, const int64_t *__restrict__ arow_slot,
-                   uint64_t *__restrict__ part, float *__restrict__ scores, int *__restrict__ err) {
+                   uint64_t *__restrict__ part, float *__restrict__ scores, uint32_t *__restrict__ qbound,
+                   int *__restrict__ err) {
     constexpr bool STORE = (S == 0);
     static_assert(!(STORE && F8), "the store mode is BF16 only");
     constexpr int SL = STORE ? 1 : 2 * S;  // list keys per query row (two column halves)
@@ -276,6 +279,12 @@ __global__ void __launch_bounds__(tc_threads(S), 1)
             for (int i = 0; i < S; ++i) L[i * TC_M] = KEY_EMPTY;
             uint64_t thr = KEY_EMPTY;  // the heap's root: the S-th best key so far
             float thr_f = __int_as_float(0x7f800000);  // +inf
+            // the query's bound from units already finished: the S-th best score of
+            // some unit's S rows, so no key above it can reach the query's S best
+            if (qbound && row < un.na) {
+                const uint32_t g = *reinterpret_cast<volatile uint32_t *>(qbound + un.a0 + row);
+                if (g != 0xffffffffu) thr_f = ord2f(g);
+            }
             // score = |x|^2 + qc * (column factor) * acc: qc = -2 (BF16) or
             // -2 scale_q (FP8, column factor scale_x)
             const float qc = F8 ? (row < un.na ? -2.f * __ldg(ascale + un.a0 + row) : 0.f) : -2.f;
@@ -390,6 +399,8 @@ __global__ void __launch_bounds__(tc_threads(S), 1)
                     uint64_t *dst = part + (arow_slot[un.a0 + row] + un.rch) * S;
 #pragma unroll 4
                     for (int i = 0; i < S; ++i) dst[i] = L[i * TC_M];
+                    // a full list bounds the query's S-th best score for later units
+                    if (qbound && thr != KEY_EMPTY) atomicMin(qbound + un.a0 + row, key_dist(thr));
                 }
             }
             asm volatile("bar.sync %0, 64;" ::"r"(1 + quad) : "memory");
@@ -428,7 +439,7 @@ int tc_topk_launch(const TcLaunch &a, cudaStream_t st) {
                                          (int)smem));
         tc_topk_kernel<Sv, Fv><<<a.grid, tc_threads(Sv), smem, st>>>(ma, mb, a.units, a.n_units, a.cta_off, a.K,
                                                                      kblk, a.bnorm, a.ascale, a.bscale, a.arow_slot,
-                                                                     a.part, a.scores, a.err);
+                                                                     a.part, a.scores, a.qbound, a.err);
         return GN_OK;
     };
     using F0 = std::false_type;
@@ -562,7 +573,7 @@ struct TcFlatState {
     int fp8 = 0;  // 0: BF16 operands; 1: FP8 E4M3 with per-row scales
     int64_t n = 0;
     DBuf x32, x16, xnorm, xscale;  // fp32 rows (dp), low-precision rows (K), |x|^2, FP8 row scales
-    DBuf q32, q16, qscale, units, nunits, ctaoff, aslot, part, err, out_idx, out_dist;
+    DBuf q32, q16, qscale, units, nunits, aslot, part, qbound, err, out_idx, out_dist;
     int64_t planned_nq = -1;
     int nchunks = 1, grid = 0;
 };
@@ -585,51 +596,55 @@ static int tcflat_lowp(TcFlatState &S, cudaStream_t st) {
     return GN_OK;
 }
 
-// Split the (query tile, database tile) space into one contiguous run per CTA,
-// cut at query-tile boundaries: each CTA keeps its per-query lists over
-// thousands of tiles, so list insertions stay rare.
+// Work units: (query tile, database chunk), chunk-major: the database is cut
+// into C chunks and every query tile's unit for chunk c comes before any unit
+// of chunk c + 1, the CTAs taking units in turn (unit u: CTA u mod grid).  So
+// the CTAs running at any moment scan the same one or two chunks: each chunk
+// comes from DRAM about once and is served to the other query tiles from L2.
+// A unit starts its lists empty, but below the query's bound published by the
+// units that finished before it (tc_topk_kernel), so later chunks insert few
+// keys.  C is chosen so that the units fill whole waves of CTAs (chunks of at
+// least 32 tiles).
 static int tcflat_plan(TcFlatState &S, int64_t nq, cudaStream_t st) {
     const int sms = dev_info().num_sms;
     const int64_t qt = ceil_div(nq, TC_M);
     const int64_t nt = ceil_div(S.n, TC_N);
-    const int64_t total = qt * nt;
-    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(sms, total));
+    int64_t C = 1;
+    double best = -1.0;
+    for (int64_t c = 1; c <= std::min<int64_t>(std::max<int64_t>(1, nt / 32), 64); ++c) {
+        const int64_t units = qt * c;
+        const double eff = (double)units / (double)(ceil_div(units, sms) * sms);
+        if (eff > best + 0.02) {  // more chunks only for a clearly fuller last wave
+            best = eff;
+            C = c;
+        }
+    }
     std::vector<TcUnit> units;
-    std::vector<int64_t> cta_off((size_t)grid + 1, 0);
-    std::vector<int32_t> seg((size_t)qt, 0);
-    for (int g = 0; g < grid; ++g) {
-        const int64_t b = total * g / grid, e = total * (g + 1) / grid;
-        int64_t p = b;
-        while (p < e) {
-            const int64_t t = p / nt;
-            const int64_t te = std::min(e, (t + 1) * nt);
+    units.reserve((size_t)(qt * C));
+    for (int64_t c = 0; c < C; ++c) {
+        const int64_t t0 = nt * c / C, t1 = nt * (c + 1) / C;
+        for (int64_t t = 0; t < qt; ++t) {
             TcUnit u{};
             u.a0 = t * TC_M;
             u.na = (int32_t)std::min<int64_t>(TC_M, nq - u.a0);
-            u.r0 = (p - t * nt) * TC_N;
-            u.r1 = std::min<int64_t>(S.n, (te - t * nt) * TC_N);
-            u.rch = seg[(size_t)t]++;
+            u.r0 = t0 * TC_N;
+            u.r1 = std::min<int64_t>(S.n, t1 * TC_N);
+            u.rch = (int32_t)c;
             units.push_back(u);
-            p = te;
         }
-        cta_off[(size_t)g + 1] = (int64_t)units.size();
     }
-    int32_t nslot = 1;
-    for (int32_t v : seg) nslot = std::max(nslot, v);
-    S.nchunks = nslot;
+    S.nchunks = (int)C;
     std::vector<int64_t> aslot((size_t)nq);
-    for (int64_t q = 0; q < nq; ++q) aslot[(size_t)q] = q * nslot;
+    for (int64_t q = 0; q < nq; ++q) aslot[(size_t)q] = q * C;
     const int64_t nu = (int64_t)units.size();
     GN_TRY(S.units.ensure(units.size() * sizeof(TcUnit)));
     GN_TRY(S.nunits.ensure(8));
-    GN_TRY(S.ctaoff.ensure(cta_off.size() * 8));
     GN_TRY(S.aslot.ensure((size_t)nq * 8));
     GN_CUDA_TRY(cudaMemcpyAsync(S.units.p, units.data(), units.size() * sizeof(TcUnit), cudaMemcpyHostToDevice, st));
     GN_CUDA_TRY(cudaMemcpyAsync(S.nunits.p, &nu, 8, cudaMemcpyHostToDevice, st));
-    GN_CUDA_TRY(cudaMemcpyAsync(S.ctaoff.p, cta_off.data(), cta_off.size() * 8, cudaMemcpyHostToDevice, st));
     GN_CUDA_TRY(cudaMemcpyAsync(S.aslot.p, aslot.data(), (size_t)nq * 8, cudaMemcpyHostToDevice, st));
     GN_CUDA_TRY(cudaStreamSynchronize(st));
-    S.grid = grid;
+    S.grid = (int)std::max<int64_t>(1, std::min<int64_t>(sms, nu));
     S.planned_nq = nq;
     return GN_OK;
 }
@@ -701,8 +716,9 @@ int gn_tcflat_search_knn_device(gn_index *ix, const float *d_queries, int64_t nq
     } else {
         to_bf16_rows(d_queries, nq, S.d, S.dp, S.q16.p, S.K, st);
     }
-    // slots of a query tile covered by fewer runs than the maximum stay empty
-    GN_CUDA_TRY(cudaMemsetAsync(S.part.p, 0xff, (size_t)nq * S.nchunks * S.S * 8, st));
+    // no bounds yet (every unit of this search publishes into them)
+    GN_TRY(S.qbound.ensure((size_t)nq * 4));
+    GN_CUDA_TRY(cudaMemsetAsync(S.qbound.p, 0xff, (size_t)nq * 4, st));
     TcLaunch a;
     a.A = S.q16.p;
     a.a_rows = std::max<int64_t>(nq, TC_M);
@@ -711,7 +727,8 @@ int gn_tcflat_search_knn_device(gn_index *ix, const float *d_queries, int64_t nq
     a.K = S.K;
     a.units = S.units.as<TcUnit>();
     a.n_units = S.nunits.as<int64_t>();
-    a.cta_off = S.ctaoff.as<int64_t>();
+    a.cta_off = nullptr;  // unit u on CTA u mod grid (chunk-major order)
+    a.qbound = S.qbound.as<uint32_t>();
     a.bnorm = S.xnorm.as<float>();
     a.arow_slot = S.aslot.as<int64_t>();
     a.part = S.part.as<uint64_t>();

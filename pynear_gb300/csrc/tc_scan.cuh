@@ -28,6 +28,8 @@ struct TcLaunch {
     const float *bnorm = nullptr;      // |B row|^2, FP32
     const int64_t *arow_slot = nullptr;
     uint64_t *part = nullptr;          // slots x S keys
+    uint32_t *qbound = nullptr;        // optional, per A row: bound of its S-th best score (ordered key;
+                                       // all ones = none), read at each unit's start, lowered at its end
     int *err = nullptr;                // device error word (0 = ok)
     int S = 40;
     int grid = 0;
