@@ -173,8 +173,9 @@ int gn_ivfl2_graph_info(gn_index *ix, int64_t *out);
  * [256,1024) [1024,4096) [4096,..) that the nq sample queries reach, times
  * every combination of rows per list-scan work unit (256/1024/4096), most
  * blocks per query selection (1/4/16) and selector threads (128/256), reps
- * runs each, and keeps the fastest.  table: 7 x {rc, bmax, nt}; zeros = the
- * built-in choice. */
+ * runs each, and keeps the fastest; then, with those fixed, the tile shape:
+ * queries per list-scan work unit, the MMA's N (32/64/128).
+ * table: 7 x {rc, bmax, nt, qc}; zeros = the built-in choice. */
 int gn_ivfl2_autotune(gn_index *ix, const float *queries, int64_t nq, int64_t k, int32_t reps, int32_t *table_out);
 int gn_ivfl2_get_tuning(gn_index *ix, int32_t *table_out);
 int gn_ivfl2_set_tuning(gn_index *ix, const int32_t *table);

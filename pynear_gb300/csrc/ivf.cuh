@@ -46,6 +46,7 @@ struct IvfL2State {
         int32_t rc = 0;    // list rows per work unit (256, 1024, 4096)
         int32_t bmax = 0;  // most blocks one query's selection is split over (1..16)
         int32_t nt = 0;    // selector threads per block (128, 256)
+        int32_t qc = 0;    // queries per list-scan work unit, the MMA's N (32, 64, 128)
     } tune[7];
     // search configuration version (bumped by every setter); CUDA graphs
     // captured for one configuration are replayed only under it

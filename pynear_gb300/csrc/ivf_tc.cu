@@ -52,7 +52,7 @@ __device__ __forceinline__ int find_list_tc(const int64_t *item_off, int nc, int
 }
 
 __device__ void tc_units_body(int64_t i, const int64_t *__restrict__ item_off, int nc,
-                              const int64_t *__restrict__ boff, const int64_t *__restrict__ list_off, int rc,
+                              const int64_t *__restrict__ boff, const int64_t *__restrict__ list_off, int rc, int qch,
                               int64_t max_units, TcUnit *__restrict__ units, int64_t *__restrict__ n_units) {
     const int64_t total = item_off[nc];
     if (i == 0) *n_units = min(total, max_units);
@@ -66,8 +66,8 @@ __device__ void tc_units_body(int64_t i, const int64_t *__restrict__ item_off, i
     // different SMs, their second and later reads of the rows hit L2
     const int64_t rch = local / nqc, qc = local % nqc;
     TcUnit u;
-    u.a0 = boff[l] + qc * TC_QCHUNK;
-    u.na = (int32_t)min((int64_t)TC_QCHUNK, boff[l + 1] - u.a0);
+    u.a0 = boff[l] + qc * qch;
+    u.na = (int32_t)min((int64_t)qch, boff[l + 1] - u.a0);
     u.r0 = lb + rch * rc;
     u.r1 = min(le, u.r0 + rc);
     u.rbase = lb;
@@ -83,7 +83,8 @@ __global__ void qb_units_kernel(const uint4 *__restrict__ q16, int K8, int np, c
                                 const int64_t *__restrict__ slot_rel, uint4 *__restrict__ qb,
                                 int64_t *__restrict__ aslot, int64_t max_pairs, unsigned qb_blocks,
                                 const int64_t *__restrict__ item_off, const int64_t *__restrict__ list_off, int rc,
-                                int64_t max_units, TcUnit *__restrict__ units, int64_t *__restrict__ n_units) {
+                                int qch, int64_t max_units, TcUnit *__restrict__ units,
+                                int64_t *__restrict__ n_units) {
     if (blockIdx.x < qb_blocks) {
         const int lane = threadIdx.x & 31;
         const int64_t pos = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
@@ -95,7 +96,7 @@ __global__ void qb_units_kernel(const uint4 *__restrict__ q16, int K8, int np, c
         return;
     }
     const int64_t i = (int64_t)(blockIdx.x - qb_blocks) * blockDim.x + threadIdx.x;
-    tc_units_body(i, item_off, nc, boff, list_off, rc, max_units, units, n_units);
+    tc_units_body(i, item_off, nc, boff, list_off, rc, qch, max_units, units, n_units);
 }
 
 
@@ -856,21 +857,24 @@ int ivfl2_search_tc(gn_index *ix, const float *dQ, int64_t nq, int k, int64_t *d
     const int rc = tn.rc ? tn.rc : (nq >= 64 ? 1024 : 256);
     // score segments in 128-row slots: slot_rel / qslot count slots, and a
     // pair's tile t has its minima at tmin4[(slot base + t) * 4 ...]
-    GN_TRY(ivf_plan(T, nq, np, S.nc, S.list_off.as<int64_t>(), rc, TC_QCHUNK, st, 128));
+    // queries per work unit (the MMA's N side): 128, or fewer to cut a mid-size
+    // batch's lists into more units
+    const int qch = tn.qc ? tn.qc : TC_QCHUNK;
+    GN_TRY(ivf_plan(T, nq, np, S.nc, S.list_off.as<int64_t>(), rc, qch, st, 128));
     const int64_t npairs = nq * np;
     const int64_t qb_rows = std::max<int64_t>(npairs, 256);  // >= one 256-row TMA box
     GN_TRY(S.qb.ensure((size_t)qb_rows * S.K * 2));
     GN_TRY(S.aslot.ensure((size_t)npairs * 8));
     const int64_t maxlen = S.top_rows.size() > 1 ? S.top_rows[1] : 0;
     // sized for the shortest row chunk (256) so that a smaller batch never needs more
-    const int64_t max_units = (ceil_div(npairs, TC_QCHUNK) + S.nc) * (ceil_div(maxlen, 256) + 1);
+    const int64_t max_units = (ceil_div(npairs, qch) + S.nc) * (ceil_div(maxlen, 256) + 1);
     GN_TRY(S.units.ensure((size_t)max_units * sizeof(TcUnit)));
     GN_TRY(S.nunits.ensure(8));
     const unsigned qb_blocks = (unsigned)ceil_div(npairs, 8);
     qb_units_kernel<<<qb_blocks + (unsigned)ceil_div(max_units, 256), 256, 0, st>>>(
         S.q16.as<uint4>(), S.K / 8, np, T.bucket.as<int64_t>(), T.boff.as<int64_t>(), S.nc, T.qslot.as<int64_t>(),
         T.slot_rel.as<int64_t>(), S.qb.as<uint4>(), S.aslot.as<int64_t>(), npairs, qb_blocks,
-        T.item_off.as<int64_t>(), S.list_off.as<int64_t>(), rc, max_units, S.units.as<TcUnit>(),
+        T.item_off.as<int64_t>(), S.list_off.as<int64_t>(), rc, qch, max_units, S.units.as<TcUnit>(),
         S.nunits.as<int64_t>());
     // score slots: at most the rows of the np largest lists per query, plus one
     // partial slot per probe

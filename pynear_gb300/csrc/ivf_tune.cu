@@ -1,6 +1,6 @@
 // ivf_tune.cu — autotuner of the tensor-core IVF engine's launch choices.
 //
-// The tensor-core engine has three launch choices whose best values depend on
+// The tensor-core engine has four launch choices whose best values depend on
 // the batch size, the list-length distribution, the probe width and the GPU:
 //   rc    list rows per work unit of the list scan (256, 1024, 4096): short
 //         units spread a small batch's few lists over all SMs, long ones cut
@@ -8,7 +8,11 @@
 //   bmax  most blocks one query's selection is split over (1, 4, 16): splitting
 //         shortens a small batch's critical path, at the price of a merge;
 //   nt    selector threads per block (128, 256): more queries resident per SM
-//         against more warps per query.
+//         against more warps per query;
+//   qc    queries per list-scan work unit, the MMA's N side (32, 64, 128): the
+//         tile shape; smaller units spread a mid-size batch's lists over more
+//         SMs at the price of more reads of each list's rows.
+// The first three are timed jointly with qc = 128, then qc with the best of them.
 // gn_ivfl2_autotune times every combination on the caller's sample queries,
 // for each batch-size bucket the sample covers ([1,4) [4,16) ... [4096,..)),
 // with CUDA events on the index's stream, and keeps the fastest per bucket in
@@ -24,6 +28,8 @@ namespace gn {
 static const int TUNE_RC[] = {256, 1024, 4096};
 static const int TUNE_BMAX[] = {1, 4, 16};
 static const int TUNE_NT[] = {128, 256};
+static const int TUNE_QC[] = {32, 64};  // besides the built-in 128
+constexpr int TUNE_COLS = 4;
 static const int64_t TUNE_NQ[7] = {2, 8, 32, 128, 512, 2048, 4096};  // representative batch per bucket
 
 }  // namespace gn
@@ -88,14 +94,36 @@ extern "C" int gn_ivfl2_autotune(gn_index *ix, const float *queries, int64_t nq,
                         best_t = S.tune[b];
                     }
                 }
+        // the tile shape, with the other choices fixed at their best (timed above
+        // with the built-in 128 queries per unit)
+        for (int qc : TUNE_QC) {
+            S.tune[b] = best_t;
+            S.tune[b].qc = qc;
+            GN_TRY(ivfl2_search_core(ix, dq.as<float>(), nb, (int)k, di.as<int64_t>(), dd.as<float>(),
+                                     dc.as<int64_t>(), st));
+            GN_CUDA_TRY(cudaEventRecord(e0, st));
+            for (int r = 0; r < reps; ++r)
+                GN_TRY(ivfl2_search_core(ix, dq.as<float>(), nb, (int)k, di.as<int64_t>(), dd.as<float>(),
+                                         dc.as<int64_t>(), st));
+            GN_CUDA_TRY(cudaEventRecord(e1, st));
+            GN_CUDA_TRY(cudaEventSynchronize(e1));
+            float ms = 0.f;
+            GN_CUDA_TRY(cudaEventElapsedTime(&ms, e0, e1));
+            if (ms < best) {
+                best = ms;
+                best_t.qc = qc;
+            }
+        }
+        if (best_t.qc == 0) best_t.qc = 128;
         S.tune[b] = best_t;
     }
     S.cfg++;  // captured graphs hold the old choices
     if (table_out)
         for (int b = 0; b < 7; ++b) {
-            table_out[3 * b] = S.tune[b].rc;
-            table_out[3 * b + 1] = S.tune[b].bmax;
-            table_out[3 * b + 2] = S.tune[b].nt;
+            table_out[TUNE_COLS * b] = S.tune[b].rc;
+            table_out[TUNE_COLS * b + 1] = S.tune[b].bmax;
+            table_out[TUNE_COLS * b + 2] = S.tune[b].nt;
+            table_out[TUNE_COLS * b + 3] = S.tune[b].qc;
         }
     return GN_OK;
 }
@@ -104,9 +132,10 @@ extern "C" int gn_ivfl2_get_tuning(gn_index *ix, int32_t *table_out) {
     if (!ix || ix->kind != K_IVFL2 || !ix->ivfl2 || !table_out) return fail(GN_ERR_INVALID, "not an IVFFlatL2 index");
     std::lock_guard<std::mutex> lk(ix->mu);
     for (int b = 0; b < 7; ++b) {
-        table_out[3 * b] = ix->ivfl2->tune[b].rc;
-        table_out[3 * b + 1] = ix->ivfl2->tune[b].bmax;
-        table_out[3 * b + 2] = ix->ivfl2->tune[b].nt;
+        table_out[TUNE_COLS * b] = ix->ivfl2->tune[b].rc;
+        table_out[TUNE_COLS * b + 1] = ix->ivfl2->tune[b].bmax;
+        table_out[TUNE_COLS * b + 2] = ix->ivfl2->tune[b].nt;
+        table_out[TUNE_COLS * b + 3] = ix->ivfl2->tune[b].qc;
     }
     return GN_OK;
 }
@@ -114,16 +143,19 @@ extern "C" int gn_ivfl2_get_tuning(gn_index *ix, int32_t *table_out) {
 extern "C" int gn_ivfl2_set_tuning(gn_index *ix, const int32_t *table) {
     if (!ix || ix->kind != K_IVFL2 || !ix->ivfl2 || !table) return fail(GN_ERR_INVALID, "not an IVFFlatL2 index");
     for (int b = 0; b < 7; ++b) {
-        const int32_t rc = table[3 * b], bm = table[3 * b + 1], nt = table[3 * b + 2];
+        const int32_t rc = table[TUNE_COLS * b], bm = table[TUNE_COLS * b + 1], nt = table[TUNE_COLS * b + 2],
+                      qc = table[TUNE_COLS * b + 3];
         if (rc && (rc < 256 || rc % 128)) return fail(GN_ERR_INVALID, "tuning: rc must be 0 or a multiple of 128 >= 256");
         if (bm < 0 || bm > 16) return fail(GN_ERR_INVALID, "tuning: bmax must be in [0, 16]");
         if (nt && nt != 128 && nt != 256) return fail(GN_ERR_INVALID, "tuning: nt must be 0, 128 or 256");
+        if (qc && qc != 32 && qc != 64 && qc != 128) return fail(GN_ERR_INVALID, "tuning: qc must be 0, 32, 64 or 128");
     }
     std::lock_guard<std::mutex> lk(ix->mu);
     for (int b = 0; b < 7; ++b) {
-        ix->ivfl2->tune[b].rc = table[3 * b];
-        ix->ivfl2->tune[b].bmax = table[3 * b + 1];
-        ix->ivfl2->tune[b].nt = table[3 * b + 2];
+        ix->ivfl2->tune[b].rc = table[TUNE_COLS * b];
+        ix->ivfl2->tune[b].bmax = table[TUNE_COLS * b + 1];
+        ix->ivfl2->tune[b].nt = table[TUNE_COLS * b + 2];
+        ix->ivfl2->tune[b].qc = table[TUNE_COLS * b + 3];
     }
     ix->ivfl2->cfg++;
     return GN_OK;

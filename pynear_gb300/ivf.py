@@ -107,21 +107,25 @@ class IVFFlatL2Index:
         """Time the tensor-core engine's launch choices on sample queries for
         every batch-size bucket the sample reaches and keep the fastest; returns
         the (7, 3) table of (rows per work unit, most blocks per query
-        selection, selector threads) per bucket.  Results are unchanged."""
+        selection, selector threads, queries per list-scan work unit) per
+        bucket.  Results are unchanged."""
         q = _f32_2d(sample_queries, "sample_queries")
-        table = np.zeros((7, 3), np.int32)
+        table = np.zeros((7, 4), np.int32)
         _lib.call("gn_ivfl2_autotune", self._h.h, _lib.ptr(q), q.shape[0], int(k), int(reps), _lib.ptr(table))
         return table
 
     @property
     def tuning(self) -> np.ndarray:
-        table = np.zeros((7, 3), np.int32)
+        table = np.zeros((7, 4), np.int32)
         _lib.call("gn_ivfl2_get_tuning", self._h.h, _lib.ptr(table))
         return table
 
     @tuning.setter
     def tuning(self, table) -> None:
-        t = np.ascontiguousarray(table, dtype=np.int32).reshape(7, 3)
+        t = np.ascontiguousarray(table, dtype=np.int32).reshape(7, -1)
+        if t.shape[1] < 4:  # a table saved without the tile column: the built-in tile
+            t = np.concatenate([t, np.zeros((7, 4 - t.shape[1]), np.int32)], axis=1)
+        t = np.ascontiguousarray(t.reshape(7, 4))
         _lib.call("gn_ivfl2_set_tuning", self._h.h, _lib.ptr(t))
 
     def last_lists_probed(self, nq: int) -> np.ndarray:

@@ -23,11 +23,11 @@ def test_autotune_table_and_results_unchanged(gn):
     ref = {n: ix.search_knn_arrays(q[:n], 10) for n in (1, 5, 40, 200, 600)}
     assert not ix.tuning.any()
     table = ix.autotune(q, 10, reps=2)
-    assert table.shape == (7, 3)
+    assert table.shape == (7, 4)
     # the 600-query sample reaches the buckets up to [256, 1024)
     for b in range(5):
-        rc, bmax, nt = table[b]
-        assert rc in (256, 1024, 4096) and bmax in (1, 4, 16) and nt in (128, 256)
+        rc, bmax, nt, qc = table[b]
+        assert rc in (256, 1024, 4096) and bmax in (1, 4, 16) and nt in (128, 256) and qc in (32, 64, 128)
     assert not table[5:].any()
     np.testing.assert_array_equal(ix.tuning, table)
     for n, r in ref.items():
@@ -39,13 +39,21 @@ def test_autotune_table_and_results_unchanged(gn):
 
 def test_tuning_table_is_checked(gn):
     ix, q = _index(gn)
-    bad = np.zeros((7, 3), np.int32)
-    bad[0] = (300, 1, 128)  # not a multiple of 128
+    bad = np.zeros((7, 4), np.int32)
+    bad[0] = (300, 1, 128, 0)  # not a multiple of 128
     with pytest.raises(ValueError):
         ix.tuning = bad
-    bad[0] = (256, 1, 64)
+    bad[0] = (256, 1, 64, 0)
     with pytest.raises(ValueError):
         ix.tuning = bad
+    bad[0] = (256, 1, 128, 48)  # no such tile
+    with pytest.raises(ValueError):
+        ix.tuning = bad
+    # a three-column table (saved before the tile column) still loads
+    old = np.zeros((7, 3), np.int32)
+    old[2] = (1024, 4, 256)
+    ix.tuning = old
+    np.testing.assert_array_equal(ix.tuning[2], (1024, 4, 256, 0))
     ix.set_engine("fp32")
     with pytest.raises(ValueError):
         ix.autotune(q, 10)
