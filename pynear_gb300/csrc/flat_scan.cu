@@ -410,17 +410,22 @@ static int launch_scan(const FlatScanArgs &a, int n_groups, int threads, size_t 
                               (uint64_t)a.stride4 * 16, (uint32_t)fg.bw, (uint32_t)fg.rows,
                               fg.bw == FS_BOX ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_NONE));
         timing_begin(st, "float_scan_kernel");
-#define GN_FLOAT_SCAN(M)                                                                                          \
-    do {                                                                                                          \
-        auto kern = float_scan_kernel<M, 4, R>;                                                                   \
-        if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); \
-        kern<<<units, threads, smem, st>>>(tm, a.n, a.d, a.stride4 * 4, reinterpret_cast<const float *>(a.q),     \
-                                           a.nq, a.k, a.n_slices, a.slice_rows, n_groups, part, a.err);           \
-    } while (0)
-        if (a.metric == M_L2) GN_FLOAT_SCAN(M_L2);
-        else if (a.metric == M_L1) GN_FLOAT_SCAN(M_L1);
-        else GN_FLOAT_SCAN(M_LINF);
-#undef GN_FLOAT_SCAN
+        auto go = [&](auto MC, auto QC) {
+            constexpr int Mv = decltype(MC)::value, Qv = decltype(QC)::value;
+            auto kern = float_scan_kernel<Mv, Qv, (Qv == 4 ? R : 1)>;
+            if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            kern<<<units, threads, smem, st>>>(tm, a.n, a.d, a.stride4 * 4, reinterpret_cast<const float *>(a.q),
+                                               a.nq, a.k, a.n_slices, a.slice_rows, n_groups, part, a.err);
+        };
+        auto by_qw = [&](auto MC) {
+            // fewer queries per warp only for small batches with k <= 32 (R == 1)
+            if (a.qw == 1 && R == 1) go(MC, std::integral_constant<int, 1>());
+            else if (a.qw == 2 && R == 1) go(MC, std::integral_constant<int, 2>());
+            else go(MC, std::integral_constant<int, 4>());
+        };
+        if (a.metric == M_L2) by_qw(std::integral_constant<int, M_L2>());
+        else if (a.metric == M_L1) by_qw(std::integral_constant<int, M_L1>());
+        else by_qw(std::integral_constant<int, M_LINF>());
         timing_end(st);
     }
     const int qpb = 4;  // queries (warps) per merge block
@@ -430,10 +435,10 @@ static int launch_scan(const FlatScanArgs &a, int n_groups, int threads, size_t 
 }
 
 // CTAs of the float scan resident per SM for this metric and list size.
-template <int M, int R>
+template <int M, int R, int QW = 4>
 static int float_scan_occupancy1(int threads, size_t smem) {
     int nb = 0;
-    auto kern = float_scan_kernel<M, 4, R>;
+    auto kern = float_scan_kernel<M, QW, R>;
     cudaError_t e = cudaSuccess;
     if (smem > 48 * 1024) e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, threads, smem);
@@ -444,7 +449,15 @@ static int float_scan_occupancy1(int threads, size_t smem) {
     return nb;
 }
 template <int R>
-static int float_scan_occupancy(int metric, int threads, size_t smem) {
+static int float_scan_occupancy(int metric, int qw, int threads, size_t smem) {
+    if (R == 1 && qw == 1)
+        return metric == M_L2 ? float_scan_occupancy1<M_L2, 1, 1>(threads, smem)
+               : metric == M_L1 ? float_scan_occupancy1<M_L1, 1, 1>(threads, smem)
+                                : float_scan_occupancy1<M_LINF, 1, 1>(threads, smem);
+    if (R == 1 && qw == 2)
+        return metric == M_L2 ? float_scan_occupancy1<M_L2, 1, 2>(threads, smem)
+               : metric == M_L1 ? float_scan_occupancy1<M_L1, 1, 2>(threads, smem)
+                                : float_scan_occupancy1<M_LINF, 1, 2>(threads, smem);
     if (metric == M_L2) return float_scan_occupancy1<M_L2, R>(threads, smem);
     if (metric == M_L1) return float_scan_occupancy1<M_L1, R>(threads, smem);
     return float_scan_occupancy1<M_LINF, R>(threads, smem);
@@ -452,7 +465,9 @@ static int float_scan_occupancy(int metric, int threads, size_t smem) {
 
 void flat_plan(FlatScanArgs &a) {
     const DevInfo &di = dev_info();
-    const int qw = (a.metric == M_HAMMING) ? 8 : 4;
+    // float metrics: four queries per warp, fewer for a small batch with
+    // k <= 32 so that every warp scores real queries
+    const int qw = (a.metric == M_HAMMING) ? 8 : (a.k <= 32 && a.nq <= 4) ? 1 : (a.k <= 32 && a.nq <= 8) ? 2 : 4;
     const size_t per_warp = (size_t)qw * a.stride4 * 16;
     int warps = 4;
     while (warps > 1 && per_warp * warps > 200 * 1024) warps >>= 1;
@@ -469,10 +484,10 @@ void flat_plan(FlatScanArgs &a) {
         // resident CTAs) whose last wave is fullest, the fewest slices on a tie
         const int threads = warps * 32;
         const size_t smem = fs_smem_bytes(warps, qw, a.stride4);
-        int occ = a.k <= 32 ? float_scan_occupancy<1>(a.metric, threads, smem)
-                  : a.k <= 64 ? float_scan_occupancy<2>(a.metric, threads, smem)
-                  : a.k <= 128 ? float_scan_occupancy<4>(a.metric, threads, smem)
-                               : float_scan_occupancy<8>(a.metric, threads, smem);
+        int occ = a.k <= 32 ? float_scan_occupancy<1>(a.metric, qw, threads, smem)
+                  : a.k <= 64 ? float_scan_occupancy<2>(a.metric, qw, threads, smem)
+                  : a.k <= 128 ? float_scan_occupancy<4>(a.metric, qw, threads, smem)
+                               : float_scan_occupancy<8>(a.metric, qw, threads, smem);
         const int64_t slots = (int64_t)std::max(occ, 1) * di.num_sms;
         const int64_t hi = std::min<int64_t>(max_slices, std::max<int64_t>(1, ceil_div(4 * slots, n_groups)));
         slices = 1;

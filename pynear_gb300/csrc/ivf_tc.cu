@@ -584,6 +584,7 @@ __global__ void __launch_bounds__(256) coarse_probe_kernel(const float *__restri
                                                            int32_t *__restrict__ probes,
                                                            int32_t *__restrict__ nprobed) {
     constexpr int NC = PROBER_CAND, H = PROBER_HIDDEN;
+    static_assert(H == 256 && NC == 64, "warp-per-row MLP layout: 32 lanes x 8 weights, 8 warps x 8 candidates");
     __shared__ int32_t sc[NC];
     __shared__ float sd[NC], sf[NC], sz[NC];
     __shared__ __align__(16) float sh1[H], sh2[H];
@@ -605,34 +606,34 @@ __global__ void __launch_bounds__(256) coarse_probe_kernel(const float *__restri
     const int ntop = block_radix_select<256>(skeys, wb, rcnt, NC, top, hist, rsh);
     if (j < NC) sc[j] = j < ntop ? (int32_t)key_idx(top[j]) : -1;
     __syncthreads();
-    {   // exact squared distances: 4 threads per candidate, float4 strides
-        const int i = j >> 2, part = j & 3;
-        const int c = sc[i];
-        float s0 = 0.f, s1 = 0.f;
-        if (c >= 0) {
-            const float4 *cr = reinterpret_cast<const float4 *>(C + (int64_t)c * dp);
-            const float4 *qr = reinterpret_cast<const float4 *>(sqr);
-            const int n4 = d >> 2;
-#pragma unroll 8
-            for (int t = part; t < n4; t += 8) {
-                const float4 a = __ldg(cr + t), b = qr[t];
-                float e0 = b.x - a.x, e1 = b.y - a.y, e2 = b.z - a.z, e3 = b.w - a.w;
-                s0 = fmaf(e0, e0, s0); s1 = fmaf(e1, e1, s1); s0 = fmaf(e2, e2, s0); s1 = fmaf(e3, e3, s1);
-                if (t + 4 < n4) {
-                    const float4 a2 = __ldg(cr + t + 4), b2 = qr[t + 4];
-                    e0 = b2.x - a2.x; e1 = b2.y - a2.y; e2 = b2.z - a2.z; e3 = b2.w - a2.w;
-                    s0 = fmaf(e0, e0, s0); s1 = fmaf(e1, e1, s1); s0 = fmaf(e2, e2, s0); s1 = fmaf(e3, e3, s1);
+    {   // exact squared distances: one warp per candidate (eight per warp), so
+        // that each load instruction reads 512 contiguous bytes of a centroid row
+        const float4 *qr = reinterpret_cast<const float4 *>(sqr);
+        const int n4 = d >> 2;
+#pragma unroll 2
+        for (int i = warp; i < NC; i += 8) {
+            const int c = sc[i];  // warp-uniform
+            float s0 = 0.f, s1 = 0.f;
+            if (c >= 0) {
+                const float4 *cr = reinterpret_cast<const float4 *>(C + (int64_t)c * dp);
+                for (int t = lane; t < n4; t += 32) {
+                    const float4 a = __ldg(cr + t), b = qr[t];
+                    const float e0 = b.x - a.x, e1 = b.y - a.y, e2 = b.z - a.z, e3 = b.w - a.w;
+                    s0 = fmaf(e0, e0, s0);
+                    s1 = fmaf(e1, e1, s1);
+                    s0 = fmaf(e2, e2, s0);
+                    s1 = fmaf(e3, e3, s1);
+                }
+                for (int t = (n4 << 2) + lane; t < d; t += 32) {  // d % 4 tail
+                    const float e = sqr[t] - C[(int64_t)c * dp + t];
+                    s0 = fmaf(e, e, s0);
                 }
             }
-            for (int t = (n4 << 2) + part; t < d; t += 4) {  // d % 4 tail
-                const float e = sqr[t] - C[(int64_t)c * dp + t];
-                s0 = fmaf(e, e, s0);
-            }
+            float sum = s0 + s1;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+            if (lane == 0) sd[i] = sum;
         }
-        float s = s0 + s1;
-        s += __shfl_xor_sync(0xffffffffu, s, 1);
-        s += __shfl_xor_sync(0xffffffffu, s, 2);
-        if (part == 0) sd[i] = s;
     }
     __syncthreads();
     if (warp == 0) {
@@ -692,52 +693,78 @@ __global__ void __launch_bounds__(256) coarse_probe_kernel(const float *__restri
     }
     sh1[j] = fmaxf(a, 0.f);
     __syncthreads();
-    // layer 2: thread j = output j, its W2 row in 16-byte loads
+    // layer 2: warp w computes outputs 32w .. 32w + 31, one W2 row (512 bytes,
+    // lane l its 16 bytes) per load instruction, four rows in flight; lane l
+    // holds h1[8l .. 8l + 7]
     {
-        const uint4 *row = reinterpret_cast<const uint4 *>(W2 + (size_t)j * H);
         const float4 *h4 = reinterpret_cast<const float4 *>(sh1);
-        float acc[4] = {0.f, 0.f, 0.f, 0.f};
-#pragma unroll 8
-        for (int v = 0; v < H / 8; ++v) {
-            const uint4 u = __ldg(row + v);
-            const __nv_bfloat162 *h = reinterpret_cast<const __nv_bfloat162 *>(&u);
-            const float4 x0 = h4[2 * v], x1 = h4[2 * v + 1];
-            const float xs[8] = {x0.x, x0.y, x0.z, x0.w, x1.x, x1.y, x1.z, x1.w};
+        const float4 x0 = h4[2 * lane], x1 = h4[2 * lane + 1];
+        const float xs[8] = {x0.x, x0.y, x0.z, x0.w, x1.x, x1.y, x1.z, x1.w};
+#pragma unroll 1
+        for (int r0 = warp * 32; r0 < warp * 32 + 32; r0 += 4) {
+            uint4 u[4];
 #pragma unroll
-            for (int e = 0; e < 4; ++e) {
-                const float2 f = __bfloat1622float2(h[e]);
-                acc[e] = fmaf(f.x, xs[2 * e], acc[e]);
-                acc[e] = fmaf(f.y, xs[2 * e + 1], acc[e]);
-            }
-        }
-        sh2[j] = fmaxf((acc[0] + acc[1]) + (acc[2] + acc[3]) + w.b2[j], 0.f);
-    }
-    __syncthreads();
-    // layer 3: 4 threads per candidate, 64 hidden units each
-    {
-        const int i = j >> 2, part = j & 3;
-        const int c = sc[i];
-        float acc = 0.f;
-        if (c >= 0) {
-            const uint4 *row = reinterpret_cast<const uint4 *>(W3 + (size_t)c * H + part * (H / 4));
-            const float4 *h4 = reinterpret_cast<const float4 *>(sh2 + part * (H / 4));
+            for (int k = 0; k < 4; ++k) u[k] = __ldg(reinterpret_cast<const uint4 *>(W2 + (size_t)(r0 + k) * H) + lane);
+            float acc[4];
 #pragma unroll
-            for (int v = 0; v < H / 32; ++v) {
-                const uint4 u = __ldg(row + v);
-                const __nv_bfloat162 *h = reinterpret_cast<const __nv_bfloat162 *>(&u);
-                const float4 x0 = h4[2 * v], x1 = h4[2 * v + 1];
-                const float xs[8] = {x0.x, x0.y, x0.z, x0.w, x1.x, x1.y, x1.z, x1.w};
+            for (int k = 0; k < 4; ++k) {
+                const __nv_bfloat162 *h = reinterpret_cast<const __nv_bfloat162 *>(&u[k]);
+                float t = 0.f;
 #pragma unroll
                 for (int e = 0; e < 4; ++e) {
                     const float2 f = __bfloat1622float2(h[e]);
-                    acc = fmaf(f.x, xs[2 * e], acc);
-                    acc = fmaf(f.y, xs[2 * e + 1], acc);
+                    t = fmaf(f.x, xs[2 * e], t);
+                    t = fmaf(f.y, xs[2 * e + 1], t);
                 }
+                acc[k] = t;
             }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+                for (int k = 0; k < 4; ++k) acc[k] += __shfl_xor_sync(0xffffffffu, acc[k], o);
+#pragma unroll
+            for (int k = 0; k < 4; ++k)
+                if (lane == k) sh2[r0 + k] = fmaxf(acc[k] + w.b2[r0 + k], 0.f);
         }
-        acc += __shfl_xor_sync(0xffffffffu, acc, 1);
-        acc += __shfl_xor_sync(0xffffffffu, acc, 2);
-        if (part == 0) sz[i] = c >= 0 ? acc + w.b3[c] : -INFINITY;
+    }
+    __syncthreads();
+    // layer 3: one warp per candidate (eight per warp, four in flight), its W3
+    // row in one load instruction
+    {
+        const float4 *h4 = reinterpret_cast<const float4 *>(sh2);
+        const float4 x0 = h4[2 * lane], x1 = h4[2 * lane + 1];
+        const float xs[8] = {x0.x, x0.y, x0.z, x0.w, x1.x, x1.y, x1.z, x1.w};
+#pragma unroll 1
+        for (int k0 = 0; k0 < 8; k0 += 4) {
+            uint4 u[4];
+            int cs[4];
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                cs[k] = sc[warp + 8 * (k0 + k)];
+                u[k] = cs[k] >= 0 ? __ldg(reinterpret_cast<const uint4 *>(W3 + (size_t)cs[k] * H) + lane)
+                                  : make_uint4(0u, 0u, 0u, 0u);
+            }
+            float acc[4];
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const __nv_bfloat162 *h = reinterpret_cast<const __nv_bfloat162 *>(&u[k]);
+                float t = 0.f;
+#pragma unroll
+                for (int e = 0; e < 4; ++e) {
+                    const float2 f = __bfloat1622float2(h[e]);
+                    t = fmaf(f.x, xs[2 * e], t);
+                    t = fmaf(f.y, xs[2 * e + 1], t);
+                }
+                acc[k] = t;
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+                for (int k = 0; k < 4; ++k) acc[k] += __shfl_xor_sync(0xffffffffu, acc[k], o);
+            if (lane == 0)
+#pragma unroll
+                for (int k = 0; k < 4; ++k) sz[warp + 8 * (k0 + k)] = cs[k] >= 0 ? acc[k] + w.b3[cs[k]] : -INFINITY;
+        }
     }
     __syncthreads();
     bool keep = false;

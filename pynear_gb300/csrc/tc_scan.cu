@@ -278,13 +278,16 @@ __global__ void __launch_bounds__(tc_threads(S), 1)
 #pragma unroll 4
             for (int i = 0; i < S; ++i) L[i * TC_M] = KEY_EMPTY;
             uint64_t thr = KEY_EMPTY;  // the heap's root: the S-th best key so far
-            float thr_f = __int_as_float(0x7f800000);  // +inf
             // the query's bound from units already finished: the S-th best score of
-            // some unit's S rows, so no key above it can reach the query's S best
+            // some unit's S rows, so no key above it can reach the query's S best;
+            // it caps the filter threshold for the whole unit (the list's own root
+            // only takes over once it is lower)
+            float gbound = __int_as_float(0x7f800000);  // +inf
             if (qbound && row < un.na) {
                 const uint32_t g = *reinterpret_cast<volatile uint32_t *>(qbound + un.a0 + row);
-                if (g != 0xffffffffu) thr_f = ord2f(g);
+                if (g != 0xffffffffu) gbound = ord2f(g);
             }
+            float thr_f = gbound;
             // score = |x|^2 + qc * (column factor) * acc: qc = -2 (BF16) or
             // -2 scale_q (FP8, column factor scale_x)
             const float qc = F8 ? (row < un.na ? -2.f * __ldg(ascale + un.a0 + row) : 0.f) : -2.f;
@@ -363,7 +366,7 @@ __global__ void __launch_bounds__(tc_threads(S), 1)
                         if (key < thr) {
                             tc_heap_replace_top(L, S, key);
                             thr = L[0];
-                            thr_f = (thr == KEY_EMPTY) ? __int_as_float(0x7f800000) : ord2f(key_dist(thr));
+                            thr_f = (thr == KEY_EMPTY) ? gbound : fminf(gbound, ord2f(key_dist(thr)));
                         }
                     }
                 }
