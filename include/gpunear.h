@@ -172,7 +172,8 @@ int gn_ivfl2_graph_info(gn_index *ix, int64_t *out);
  * unchanged): for each batch-size bucket [1,4) [4,16) [16,64) [64,256)
  * [256,1024) [1024,4096) [4096,..) that the nq sample queries reach, times
  * every combination of rows per list-scan work unit (256/1024/4096), most
- * blocks per query selection (1/4/16) and selector threads (128/256), reps
+ * blocks per query selection (1/4/16) and selector threads per query (32 =
+ * one warp, 128/256 = a block), reps
  * runs each, and keeps the fastest; then, with those fixed, the tile shape:
  * queries per list-scan work unit, the MMA's N (32/64/128).
  * table: 7 x {rc, bmax, nt, qc}; zeros = the built-in choice. */

@@ -550,6 +550,201 @@ __global__ void __launch_bounds__(NT, 1024 / NT) ivf_tc_select_kernel(
     if (lane == 0 && out_cnt) out_cnt[q] = cnt;
 }
 
+// Selection of one query per warp, for large batches (no block barriers): the
+// same keys (score, row), the same S smallest, the same exact re-rank and
+// output as ivf_tc_select_kernel.
+//   threshold  tau = the S-th smallest quarter minimum of the query's first 64
+//              slots (a bitwise select over the warp's 256 values): S distinct
+//              rows score <= tau;
+//   sweep      the block kernel's warp loop over all the query's slots: 8
+//              slots a step, only quarters whose minimum is <= tau are read,
+//              their scores <= the warp threshold buffered as keys;
+//   select     bitonic sort of the buffer (a full buffer is cut to its best S
+//              on the way), the first S keys;
+//   re-rank    two rows at a time (rows prefetched into L2 first), then the k
+//              nearest, ties to the lower original index.
+// Needs np <= 64 probes.
+constexpr int SELW_WARPS = 4;
+
+__global__ void __launch_bounds__(32 * SELW_WARPS) ivf_tc_select_warp_kernel(
+    const float *__restrict__ scores, const uint4 *__restrict__ tmin4, const int32_t *__restrict__ probes, int np,
+    const int64_t *__restrict__ qseg, const int64_t *__restrict__ seg_rel, const int64_t *__restrict__ list_off,
+    int S, const float *__restrict__ Q, const float *__restrict__ X, int d, int dp, const int32_t *__restrict__ ids,
+    int64_t nq, int k, int64_t *__restrict__ out_idx, float *__restrict__ out_dist, int64_t *__restrict__ out_cnt) {
+    __shared__ uint64_t wreg[SELW_WARPS * SEL_WB];
+    __shared__ int64_t w_pre[SELW_WARPS][65], w_lb[SELW_WARPS][64], w_len[SELW_WARPS][64], w_sb[SELW_WARPS][64];
+    __shared__ uint64_t w_rk[SELW_WARPS][64];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int64_t q = (int64_t)blockIdx.x * SELW_WARPS + warp;
+    if (q >= nq) return;  // the whole warp; no block barrier below
+    uint64_t *W = wreg + warp * SEL_WB;
+    int64_t *pre = w_pre[warp], *plb = w_lb[warp], *plen = w_len[warp], *psb = w_sb[warp];
+    // probes: lane l holds probes l and l + 32; the slot counts' prefix sum in probe order
+    int64_t ns[2];
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        const int p = h * 32 + lane;
+        ns[h] = 0;
+        plb[p] = 0;
+        plen[p] = 0;
+        psb[p] = 0;
+        const int32_t l = p < np ? probes[q * np + p] : -1;
+        if (l >= 0) {
+            plb[p] = list_off[l];
+            plen[p] = list_off[l + 1] - plb[p];
+            psb[p] = qseg[q] + seg_rel[q * np + p];
+            ns[h] = (plen[p] + 127) >> 7;
+        }
+    }
+    int64_t inc0 = ns[0], inc1 = ns[1];
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int64_t a = __shfl_up_sync(0xffffffffu, inc0, o), b = __shfl_up_sync(0xffffffffu, inc1, o);
+        if (lane >= o) {
+            inc0 += a;
+            inc1 += b;
+        }
+    }
+    const int64_t tot0 = __shfl_sync(0xffffffffu, inc0, 31);
+    inc1 += tot0;
+    pre[lane + 1] = inc0;
+    pre[lane + 33] = inc1;
+    if (lane == 0) pre[0] = 0;
+    __syncwarp();
+    const int64_t all = pre[64];
+    // threshold from the quarter minima of the first (up to) 64 slots
+    uint32_t mv[8];
+    const int64_t nfirst = min(all, (int64_t)64);
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        const int64_t f = h * 32 + lane;
+        uint4 m4 = make_uint4(0xffffffffu, 0xffffffffu, 0xffffffffu, 0xffffffffu);
+        if (f < nfirst) {
+            int lo = 0, hi = 64;  // the probe whose slots hold f: pre[p] <= f < pre[p + 1]
+            while (hi - lo > 1) {
+                const int mid = (lo + hi) >> 1;
+                if (pre[mid] <= f) lo = mid;
+                else hi = mid;
+            }
+            m4 = __ldg(tmin4 + psb[lo] + (f - pre[lo]));
+        }
+        mv[4 * h] = m4.x;
+        mv[4 * h + 1] = m4.y;
+        mv[4 * h + 2] = m4.z;
+        mv[4 * h + 3] = m4.w;
+    }
+    uint32_t tau = 0xffffffffu;
+    if (4 * nfirst >= S) {
+        tau = 0;
+        for (int b = 31; b >= 0; --b) {
+            const uint32_t t = tau | ((1u << b) - 1u);
+            int cnt = 0;
+#pragma unroll
+            for (int u = 0; u < 8; ++u) cnt += __popc(__ballot_sync(0xffffffffu, mv[u] <= t));
+            if (cnt < S) tau |= 1u << b;
+        }
+    }
+    uint64_t wthr = tau == 0xffffffffu ? KEY_EMPTY : make_key(tau, 0xffffffffu);
+    int wn = 0;
+    int p = 0;  // probe of this lane's slot (monotone over the sweep)
+    for (int64_t g0 = 0; g0 < all; g0 += 8) {
+        const int64_t f = g0 + (lane >> 2);
+        const int qu = lane & 3;
+        bool qual = false;
+        if (f < all) {
+            while (pre[p + 1] <= f) ++p;
+            qual = __ldg(reinterpret_cast<const uint32_t *>(tmin4 + psb[p] + (f - pre[p])) + qu) <= tau;
+        }
+        unsigned bal = __ballot_sync(0xffffffffu, qual);
+        while (bal) {
+            // up to four qualifying quarters at a time, their loads in flight together
+            int src[4], nb = 0;
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                src[u] = bal ? __ffs(bal) - 1 : -1;
+                if (bal) {
+                    bal &= bal - 1;
+                    ++nb;
+                }
+            }
+            uint64_t key[4];
+            bool want[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const int sl = src[u] < 0 ? 0 : src[u];
+                const int pp = __shfl_sync(0xffffffffu, p, sl);
+                const int64_t slot = g0 + (sl >> 2) - pre[pp];
+                const int i = (sl & 3) * 32 + lane;  // row within the slot
+                const int64_t r0 = slot * 128;
+                const bool ok = u < nb && r0 + i < plen[pp];
+                const uint32_t v = ok ? f2ord(__ldg(scores + (psb[pp] + slot) * 128 + i)) : 0xffffffffu;
+                key[u] = make_key(v, (uint32_t)(plb[pp] + r0 + i));
+                want[u] = ok;
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                bool w = want[u] && key[u] < wthr;
+                while (true) {
+                    const unsigned b2 = __ballot_sync(0xffffffffu, w);
+                    if (!b2) break;
+                    const int pos = wn + __popc(b2 & ((1u << lane) - 1u));
+                    if (w && pos < SEL_WB) {
+                        W[pos] = key[u];
+                        w = false;
+                    }
+                    wn += __popc(b2);
+                    if (wn <= SEL_WB) break;
+                    // full: keep the best S; keys that did not fit are offered again
+                    __syncwarp();
+                    warp_bitonic_sort(W, SEL_WB, lane);
+                    wthr = W[S - 1];
+                    wn = S;
+                    w = w && key[u] < wthr;
+                    __syncwarp();
+                }
+            }
+        }
+    }
+    // the S best of the buffer: sort it (padded to a power of two)
+    int P = 32;
+    while (P < wn) P <<= 1;
+    for (int i = wn + lane; i < P; i += 32) W[i] = KEY_EMPTY;
+    __syncwarp();
+    warp_bitonic_sort(W, P, lane);
+    const int m = min(S, wn);
+    // exact re-rank; every candidate row prefetched into L2 first
+    const float *qrow = Q + q * dp;
+    {
+        const int lines = (d * 4 + 127) / 128;
+        for (int i = lane; i < m * lines; i += 32)
+            asm volatile("prefetch.global.L2 [%0];" ::"l"(X + (int64_t)key_idx(W[i / lines]) * dp + (i % lines) * 32));
+    }
+    for (int r = 0; r < m; r += 2) {
+        int64_t rows[2] = {(int64_t)key_idx(W[r]), r + 1 < m ? (int64_t)key_idx(W[r + 1]) : -1};
+        const int n = r + 1 < m ? 2 : 1;
+        float dd[2];
+        l2sq_warp_rows(qrow, X, dp, d, rows, n, dd, lane);
+        if (lane == 0)
+            for (int u = 0; u < n; ++u) w_rk[warp][r + u] = make_key(__float_as_uint(dd[u]), (uint32_t)ids[rows[u]]);
+    }
+    __syncwarp();
+    WarpTopK<1> F;
+    F.init();
+    uint64_t fthr = KEY_EMPTY;
+    for (int r0 = 0; r0 < S; r0 += 32) {
+        const uint64_t key = (r0 + lane < m) ? w_rk[warp][r0 + lane] : KEY_EMPTY;
+        F.offer(key, fthr, k);
+    }
+    const uint64_t key = F.v[0];
+    const bool e = key == KEY_EMPTY;
+    if (lane < k) {
+        out_idx[q * k + lane] = e ? -1 : (int64_t)key_idx(key);
+        out_dist[q * k + lane] = e ? 0.f : __uint_as_float(key_dist(key));
+    }
+    const int cnt = __popc(__ballot_sync(0xffffffffu, lane < k && !e));
+    if (lane == 0 && out_cnt) out_cnt[q] = cnt;
+}
+
 // ── tensor-core coarse stage ──────────────────────────────────────────────
 // Units of the centroid scan: every query chunk of 256 against every chunk of
 // 128 centroids; aslot[q] = q * nc so the scores land row-major [nq x nc].
@@ -934,8 +1129,18 @@ int ivfl2_search_tc(gn_index *ix, const float *dQ, int64_t nq, int k, int64_t *d
     timing_begin(st, "tc_ivf_kernel");
     GN_TRY(tc_ivf_launch(a, st));
     timing_end(st);
-    // B blocks per query: split small batches so that they still fill the GPU
+    // selector: a warp per query for large batches (the autotuner's nt = 32,
+    // by default from 1,024 queries), else blocks of nt threads per query
     const int nsm = dev_info().num_sms;
+    if (np <= 64 && (tn.nt ? tn.nt == 32 : nq >= 1024)) {
+        ivf_tc_select_warp_kernel<<<(unsigned)ceil_div(nq, SELW_WARPS), 32 * SELW_WARPS, 0, st>>>(
+            S.scores.as<float>(), S.tmin.as<uint4>(), T.probes.as<int32_t>(), np, T.qslot.as<int64_t>(),
+            T.slot_rel.as<int64_t>(), S.list_off.as<int64_t>(), S.shortlist, dQ, S.vecs.as<float>(), S.d, S.dp,
+            S.ids.as<int32_t>(), nq, k, d_idx, d_dist, d_cnt);
+        GN_CUDA_TRY(cudaGetLastError());
+        return GN_OK;
+    }
+    // B blocks per query: split small batches so that they still fill the GPU
     int B = 1;
     const int bmax = tn.bmax ? tn.bmax : 16;
     if (np <= SEL_PCH)
@@ -964,7 +1169,7 @@ int ivfl2_search_tc(gn_index *ix, const float *dQ, int64_t nq, int k, int64_t *d
             S.sel_part.as<uint64_t>(), S.sel_done.as<int>(), d_idx, d_dist, d_cnt);
         return GN_OK;
     };
-    if (tn.nt ? tn.nt == 128 : nq * B >= (int64_t)nsm * 8) GN_TRY(sel(std::integral_constant<int, 128>()));
+    if (tn.nt == 128 || (tn.nt != 256 && nq * B >= (int64_t)nsm * 8)) GN_TRY(sel(std::integral_constant<int, 128>()));
     else GN_TRY(sel(std::integral_constant<int, 256>()));
     GN_CUDA_TRY(cudaGetLastError());
     return GN_OK;

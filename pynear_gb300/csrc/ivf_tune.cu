@@ -7,8 +7,9 @@
 //         per-unit overhead;
 //   bmax  most blocks one query's selection is split over (1, 4, 16): splitting
 //         shortens a small batch's critical path, at the price of a merge;
-//   nt    selector threads per block (128, 256): more queries resident per SM
-//         against more warps per query;
+//   nt    selector threads per query (32, 128, 256): 32 is one warp per query
+//         (no block barriers, for large batches), 128 and 256 a block of that
+//         many threads per query (part);
 //   qc    queries per list-scan work unit, the MMA's N side (32, 64, 128): the
 //         tile shape; smaller units spread a mid-size batch's lists over more
 //         SMs at the price of more reads of each list's rows.
@@ -27,7 +28,7 @@ namespace gn {
 
 static const int TUNE_RC[] = {256, 1024, 4096};
 static const int TUNE_BMAX[] = {1, 4, 16};
-static const int TUNE_NT[] = {128, 256};
+static const int TUNE_NT[] = {32, 128, 256};  // 32: one warp per query
 static const int TUNE_QC[] = {32, 64};  // besides the built-in 128
 constexpr int TUNE_COLS = 4;
 static const int64_t TUNE_NQ[7] = {2, 8, 32, 128, 512, 2048, 4096};  // representative batch per bucket
@@ -74,8 +75,9 @@ extern "C" int gn_ivfl2_autotune(gn_index *ix, const float *queries, int64_t nq,
         for (int rc : TUNE_RC)
             for (int bm : TUNE_BMAX)
                 for (int nt : TUNE_NT) {
-                    // a split the batch never uses would time the same launch again
-                    if (bm > 1 && nb * 2 > (int64_t)nsm * 4) continue;
+                    // a split the batch never uses would time the same launch again (the
+                    // warp-per-query selector never splits)
+                    if (bm > 1 && (nb * 2 > (int64_t)nsm * 4 || nt == 32)) continue;
                     S.tune[b].rc = rc;
                     S.tune[b].bmax = bm;
                     S.tune[b].nt = nt;
@@ -147,7 +149,8 @@ extern "C" int gn_ivfl2_set_tuning(gn_index *ix, const int32_t *table) {
                       qc = table[TUNE_COLS * b + 3];
         if (rc && (rc < 256 || rc % 128)) return fail(GN_ERR_INVALID, "tuning: rc must be 0 or a multiple of 128 >= 256");
         if (bm < 0 || bm > 16) return fail(GN_ERR_INVALID, "tuning: bmax must be in [0, 16]");
-        if (nt && nt != 128 && nt != 256) return fail(GN_ERR_INVALID, "tuning: nt must be 0, 128 or 256");
+        if (nt && nt != 32 && nt != 128 && nt != 256)
+            return fail(GN_ERR_INVALID, "tuning: nt must be 0, 32, 128 or 256");
         if (qc && qc != 32 && qc != 64 && qc != 128) return fail(GN_ERR_INVALID, "tuning: qc must be 0, 32, 64 or 128");
     }
     std::lock_guard<std::mutex> lk(ix->mu);

@@ -27,7 +27,7 @@ def test_autotune_table_and_results_unchanged(gn):
     # the 600-query sample reaches the buckets up to [256, 1024)
     for b in range(5):
         rc, bmax, nt, qc = table[b]
-        assert rc in (256, 1024, 4096) and bmax in (1, 4, 16) and nt in (128, 256) and qc in (32, 64, 128)
+        assert rc in (256, 1024, 4096) and bmax in (1, 4, 16) and nt in (32, 128, 256) and qc in (32, 64, 128)
     assert not table[5:].any()
     np.testing.assert_array_equal(ix.tuning, table)
     for n, r in ref.items():
@@ -43,7 +43,7 @@ def test_tuning_table_is_checked(gn):
     bad[0] = (300, 1, 128, 0)  # not a multiple of 128
     with pytest.raises(ValueError):
         ix.tuning = bad
-    bad[0] = (256, 1, 64, 0)
+    bad[0] = (256, 1, 64, 0)  # no such selector width
     with pytest.raises(ValueError):
         ix.tuning = bad
     bad[0] = (256, 1, 128, 48)  # no such tile
@@ -57,3 +57,29 @@ def test_tuning_table_is_checked(gn):
     ix.set_engine("fp32")
     with pytest.raises(ValueError):
         ix.autotune(q, 10)
+
+
+@pytest.mark.parametrize("shortlist", [16, 40, 64])
+def test_selector_widths_give_identical_results(gn, shortlist):
+    """The warp-per-query selector (tuning nt = 32) and the block selectors
+    (128, 256 threads, split or not) return the same rows and distances, bit
+    for bit, with fixed probing and with more probes than one warp's lanes."""
+    rng = np.random.default_rng(50 + shortlist)
+    c = rng.standard_normal((200, 96), dtype=np.float32)
+    db = (c[rng.integers(0, 200, 50000)] + np.float32(0.35) * rng.standard_normal((50000, 96), dtype=np.float32))
+    q = (c[rng.integers(0, 200, 700)] + np.float32(0.35) * rng.standard_normal((700, 96), dtype=np.float32))
+    ix = gn.IVFFlatL2Index(n_clusters=128, n_probe=7, engine="tc", shortlist=shortlist)
+    ix.set(db)
+    k = min(10, shortlist)
+    for nprobe in (7, 48):
+        ix.n_probe = nprobe
+        results = {}
+        for nt in (32, 128, 256):
+            t = np.zeros((7, 4), np.int32)
+            t[:, 2] = nt
+            ix.tuning = t
+            results[nt] = [ix.search_knn_arrays(q[:n], k) for n in (1, 33, 700)]
+        for nt in (128, 256):
+            for got, ref in zip(results[nt], results[32]):
+                for a, b in zip(got, ref):
+                    np.testing.assert_array_equal(a, b)
