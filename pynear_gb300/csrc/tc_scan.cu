@@ -21,9 +21,10 @@
 //              first reduced to its minimum, which is compared with the
 //              threshold (the heap's root, and the other half's root): most
 //              blocks end there, the rest are filtered score by score.
-// At the end of a unit each query's S keys go to its partial slot, and a full
-// list's S-th best score is published as the query's bound (atomicMin), below
-// which later units of the query filter from their start; the re-rank kernel
+// At the end of a unit each query's S keys go to its partial slot.  A full
+// list's S-th best score is published as the query's bound (atomicMin) every
+// tile, and every tile reads it back, so the units of a query that run at the
+// same time (its other database chunks) and later ones filter below it; the re-rank kernel
 // merges a query's slots, keeps the S best by BF16 score, recomputes their
 // distances exactly in FP32 and returns the k nearest.
 #include <cuda_bf16.h>
@@ -296,6 +297,10 @@ __global__ void __launch_bounds__(tc_threads(S), 1)
                 const int b = tile_it & 1;
                 const uint32_t tph = (tile_it >> 1) & 1;
                 const int64_t n0 = un.r0 + (int64_t)t * TC_N;
+                // the query's bound as the units running beside this one (its other
+                // database chunks) have lowered it so far, read before the wait
+                uint32_t gnow = 0xffffffffu;
+                if (qbound && row < un.na) gnow = *reinterpret_cast<volatile uint32_t *>(qbound + un.a0 + row);
                 // row norms of this warp's 128 columns, fetched before the wait
                 float nrm[TC_N / 64], csc[TC_N / 64];
 #pragma unroll
@@ -306,12 +311,20 @@ __global__ void __launch_bounds__(tc_threads(S), 1)
                 }
                 if (!mbar_wait(accfull + b, tph, verr)) { ok = false; break; }
                 tc_fence_after();
+                if (gnow != 0xffffffffu) {
+                    gbound = fminf(gbound, ord2f(gnow));
+                    thr_f = fminf(thr_f, gbound);
+                }
                 // the other half's S-th best also bounds this row: a key not below
                 // it has S better keys in the other half
                 {
                     const uint64_t o = *other_root;
                     if (o != KEY_EMPTY) thr_f = fminf(thr_f, ord2f(key_dist(o)));
                 }
+                // publish this half's S-th best (once its list is full) for the
+                // query's other units
+                if (qbound && thr != KEY_EMPTY && row < un.na && key_dist(thr) < gnow)
+                    atomicMin(qbound + un.a0 + row, key_dist(thr));
 #pragma unroll 1
                 for (int cc = 0; cc < TC_N / 64; ++cc) {
                     const int c = half * (TC_N / 64) + cc;
