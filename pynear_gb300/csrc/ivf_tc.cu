@@ -550,7 +550,7 @@ __global__ void __launch_bounds__(NT, 1024 / NT) ivf_tc_select_kernel(
     if (lane == 0 && out_cnt) out_cnt[q] = cnt;
 }
 
-// Selection of one query per warp, for large batches (no block barriers): the
+// Selection of one query per warp (no block barriers; an autotuner option): the
 // same keys (score, row), the same S smallest, the same exact re-rank and
 // output as ivf_tc_select_kernel.
 //   threshold  tau = the S-th smallest quarter minimum of the query's first 64
@@ -1129,10 +1129,12 @@ int ivfl2_search_tc(gn_index *ix, const float *dQ, int64_t nq, int k, int64_t *d
     timing_begin(st, "tc_ivf_kernel");
     GN_TRY(tc_ivf_launch(a, st));
     timing_end(st);
-    // selector: a warp per query for large batches (the autotuner's nt = 32,
-    // by default from 1,024 queries), else blocks of nt threads per query
+    // selector: a warp per query when the autotuner chose it (nt = 32; it
+    // measured slower than the block selectors on the 1M x 512 mixture, whose
+    // queries probe ~300 slots each: one warp sweeps them one dependent load
+    // after another), else blocks of nt threads per query
     const int nsm = dev_info().num_sms;
-    if (np <= 64 && (tn.nt ? tn.nt == 32 : nq >= 1024)) {
+    if (np <= 64 && tn.nt == 32) {
         ivf_tc_select_warp_kernel<<<(unsigned)ceil_div(nq, SELW_WARPS), 32 * SELW_WARPS, 0, st>>>(
             S.scores.as<float>(), S.tmin.as<uint4>(), T.probes.as<int32_t>(), np, T.qslot.as<int64_t>(),
             T.slot_rel.as<int64_t>(), S.list_off.as<int64_t>(), S.shortlist, dQ, S.vecs.as<float>(), S.d, S.dp,
