@@ -30,7 +30,12 @@ struct IvfL2State {
     int mode = 0;                // 0 FP32 CUDA-core scan, 1 BF16 tcgen05 shortlist + exact FP32 re-rank
     int shortlist = 40;
     int K = 0;                   // BF16 row length, round_up(d, 64)
-    DBuf x16;                    // n*K BF16 rows, list order
+    DBuf x16;                    // BF16 rows in list order, tiled: every list padded to a multiple of
+                                 // 128 rows (list l from padded row xoff[l]); the 128 rows of a tile
+                                 // stored K-slice by K-slice, each slice (128 rows x 64 values, 16 KB)
+                                 // contiguous, so one TMA box is one contiguous block
+    DBuf xoff;                   // int64 nc + 1: padded start row of each list in x16
+    int64_t x16_rows = 0;        // padded rows
     DBuf qb, aslot, units, nunits, err, scores;
     DBuf sel_part, sel_done;     // split selection: partial best-S lists, per-query arrival counters
     DBuf sched;                  // unit counters of the tensor-core scans (coarse, lists)

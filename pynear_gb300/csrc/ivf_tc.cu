@@ -52,8 +52,9 @@ __device__ __forceinline__ int find_list_tc(const int64_t *item_off, int nc, int
 }
 
 __device__ void tc_units_body(int64_t i, const int64_t *__restrict__ item_off, int nc,
-                              const int64_t *__restrict__ boff, const int64_t *__restrict__ list_off, int rc, int qch,
-                              int64_t max_units, TcUnit *__restrict__ units, int64_t *__restrict__ n_units) {
+                              const int64_t *__restrict__ boff, const int64_t *__restrict__ list_off,
+                              const int64_t *__restrict__ xoff, int rc, int qch, int64_t max_units,
+                              TcUnit *__restrict__ units, int64_t *__restrict__ n_units) {
     const int64_t total = item_off[nc];
     if (i == 0) *n_units = min(total, max_units);
     if (i >= total || i >= max_units) return;
@@ -71,6 +72,7 @@ __device__ void tc_units_body(int64_t i, const int64_t *__restrict__ item_off, i
     u.r0 = lb + rch * rc;
     u.r1 = min(le, u.r0 + rc);
     u.rbase = lb;
+    u.xrow = xoff[l] + (u.r0 - lb);  // rc is a multiple of 128: stays tile-aligned
     u.rch = (int32_t)rch;
     units[i] = u;
 }
@@ -82,9 +84,9 @@ __global__ void qb_units_kernel(const uint4 *__restrict__ q16, int K8, int np, c
                                 const int64_t *__restrict__ boff, int nc, const int64_t *__restrict__ qslot,
                                 const int64_t *__restrict__ slot_rel, uint4 *__restrict__ qb,
                                 int64_t *__restrict__ aslot, int64_t max_pairs, unsigned qb_blocks,
-                                const int64_t *__restrict__ item_off, const int64_t *__restrict__ list_off, int rc,
-                                int qch, int64_t max_units, TcUnit *__restrict__ units,
-                                int64_t *__restrict__ n_units) {
+                                const int64_t *__restrict__ item_off, const int64_t *__restrict__ list_off,
+                                const int64_t *__restrict__ xoff, int rc, int qch, int64_t max_units,
+                                TcUnit *__restrict__ units, int64_t *__restrict__ n_units) {
     if (blockIdx.x < qb_blocks) {
         const int lane = threadIdx.x & 31;
         const int64_t pos = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
@@ -96,7 +98,7 @@ __global__ void qb_units_kernel(const uint4 *__restrict__ q16, int K8, int np, c
         return;
     }
     const int64_t i = (int64_t)(blockIdx.x - qb_blocks) * blockDim.x + threadIdx.x;
-    tc_units_body(i, item_off, nc, boff, list_off, rc, qch, max_units, units, n_units);
+    tc_units_body(i, item_off, nc, boff, list_off, xoff, rc, qch, max_units, units, n_units);
 }
 
 
@@ -762,6 +764,7 @@ __global__ void coarse_units_kernel(int64_t nq, int nc, TcUnit *__restrict__ uni
     u.r0 = cc * 128;
     u.r1 = min((int64_t)nc, u.r0 + 128);
     u.rbase = 0;
+    u.xrow = u.r0;
     u.rch = 0;
     units[t] = u;
 }
@@ -1045,13 +1048,51 @@ static int ivfl2_probes_tc(gn_index *ix, const float *dQ, int64_t nq, int *np_ou
     return GN_OK;
 }
 
+// FP32 list rows (dp floats) -> the tiled BF16 layout of IvfL2State::x16:
+// thread per (row, 8 values); row r of list l goes to padded row
+// p = xoff[l] + (r - list_off[l]), tile p / 128, and its K slice kb to the
+// 16 KB block (tile * K/64 + kb); values past d are zero.
+__global__ void x16_tiled_kernel(const float *__restrict__ X, int64_t n, int d, int dp,
+                                 const int64_t *__restrict__ list_off, int nc, const int64_t *__restrict__ xoff,
+                                 int K, uint4 *__restrict__ out) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int g8 = K / 8;
+    const int64_t r = t / g8;
+    if (r >= n) return;
+    const int g = (int)(t % g8);
+    int lo = 0, hi = nc;  // list l: list_off[l] <= r < list_off[l + 1]
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (list_off[mid] <= r) lo = mid;
+        else hi = mid;
+    }
+    const int64_t p = xoff[lo] + (r - list_off[lo]);
+    const int kb = g >> 3, e0 = (g & 7) * 8, c0 = kb * 64 + e0;
+    __align__(16) __nv_bfloat16 v[8];
+#pragma unroll
+    for (int e = 0; e < 8; ++e) v[e] = __float2bfloat16_rn(c0 + e < d ? X[r * dp + c0 + e] : 0.f);
+    out[((((p >> 7) * (K / 64) + kb) * 128 + (p & 127)) * 64 + e0) / 8] = *reinterpret_cast<const uint4 *>(v);
+}
+
 int ivfl2_prepare_tc(gn_index *ix, cudaStream_t st) {
     IvfL2State &S = *ix->ivfl2;
     S.K = (int)round_up(S.d, 64);
-    const int64_t rows = std::max<int64_t>(S.n, 256);  // at least one 256-row TMA box
-    GN_TRY(S.x16.ensure((size_t)rows * S.K * 2));
-    GN_CUDA_TRY(cudaMemsetAsync(S.x16.p, 0, (size_t)rows * S.K * 2, st));
-    to_bf16_rows(S.vecs.as<float>(), S.n, S.d, S.dp, S.x16.p, S.K, st);
+    // BF16 list rows, tiled (see IvfL2State::x16): padded list starts
+    std::vector<int64_t> xo((size_t)S.nc + 1, 0);
+    for (int32_t l = 0; l < S.nc; ++l)
+        xo[(size_t)l + 1] = xo[(size_t)l] + round_up(S.h_off[(size_t)l + 1] - S.h_off[(size_t)l], 128);
+    S.x16_rows = std::max<int64_t>(xo[(size_t)S.nc], 128);
+    if (S.x16_rows * (S.K / 64) >= ((int64_t)1 << 31))
+        return fail(GN_ERR_UNSUPPORTED, "tensor-core IVF: too many rows x dimensions for the tiled layout");
+    GN_TRY(S.xoff.ensure(xo.size() * 8));
+    GN_CUDA_TRY(cudaMemcpyAsync(S.xoff.p, xo.data(), xo.size() * 8, cudaMemcpyHostToDevice, st));
+    GN_TRY(S.x16.ensure((size_t)S.x16_rows * S.K * 2));
+    GN_CUDA_TRY(cudaMemsetAsync(S.x16.p, 0, (size_t)S.x16_rows * S.K * 2, st));
+    if (S.n > 0)
+        x16_tiled_kernel<<<(unsigned)ceil_div(S.n * (S.K / 8), 256), 256, 0, st>>>(
+            S.vecs.as<float>(), S.n, S.d, S.dp, S.list_off.as<int64_t>(), S.nc, S.xoff.as<int64_t>(), S.K,
+            S.x16.as<uint4>());
+    GN_CUDA_TRY(cudaStreamSynchronize(st));  // xo goes out of scope
     const int64_t crows = std::max<int64_t>(S.nc, 128);  // at least one 128-row TMA box
     GN_TRY(S.c16.ensure((size_t)crows * S.K * 2));
     GN_CUDA_TRY(cudaMemsetAsync(S.c16.p, 0, (size_t)crows * S.K * 2, st));
@@ -1096,7 +1137,7 @@ int ivfl2_search_tc(gn_index *ix, const float *dQ, int64_t nq, int k, int64_t *d
     qb_units_kernel<<<qb_blocks + (unsigned)ceil_div(max_units, 256), 256, 0, st>>>(
         S.q16.as<uint4>(), S.K / 8, np, T.bucket.as<int64_t>(), T.boff.as<int64_t>(), S.nc, T.qslot.as<int64_t>(),
         T.slot_rel.as<int64_t>(), S.qb.as<uint4>(), S.aslot.as<int64_t>(), npairs, qb_blocks,
-        T.item_off.as<int64_t>(), S.list_off.as<int64_t>(), rc, qch, max_units, S.units.as<TcUnit>(),
+        T.item_off.as<int64_t>(), S.list_off.as<int64_t>(), S.xoff.as<int64_t>(), rc, qch, max_units, S.units.as<TcUnit>(),
         S.nunits.as<int64_t>());
     // score slots: at most the rows of the np largest lists per query, plus one
     // partial slot per probe
@@ -1106,7 +1147,8 @@ int ivfl2_search_tc(gn_index *ix, const float *dQ, int64_t nq, int k, int64_t *d
     GN_TRY(S.tmin.ensure((size_t)std::max<int64_t>(slots_total, 1) * 4 * 4));
     TcIvfLaunch a;
     a.X = S.x16.p;
-    a.x_rows = std::max<int64_t>(S.n, 256);
+    a.x_rows = S.x16_rows;
+    a.tiled = 1;
     a.Q = S.qb.p;
     a.q_rows = qb_rows;
     a.K = S.K;

@@ -6,7 +6,8 @@
 namespace gn {
 
 struct TcIvfLaunch {
-    const void *X = nullptr;  // BF16 list rows [x_rows x K] (x_rows >= 128)
+    const void *X = nullptr;  // BF16 rows [x_rows x K] (x_rows >= 128), plain or (tiled) as IvfL2State::x16
+    int tiled = 0;            // X in the tiled layout: units address it by TcUnit::xrow
     int64_t x_rows = 0;
     const void *Q = nullptr;  // BF16 query rows in bucket order [q_rows x K] (q_rows >= 256)
     int64_t q_rows = 0;

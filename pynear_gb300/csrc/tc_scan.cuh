@@ -12,6 +12,7 @@ struct TcUnit {
     int64_t r0;
     int64_t r1;
     int64_t rbase;  // store mode: first B row of the list the unit belongs to
+    int64_t xrow;   // IVF list scan, tiled row layout: the padded row of r0 (a multiple of 128)
     int32_t na;
     int32_t rch;
 };
