@@ -40,7 +40,6 @@ constexpr int TI_SET = 8;     // warps per set (4 TMEM lane quadrants x 2 column
 constexpr int TI_NACC = 4;    // TMEM accumulators of TI_NMAX columns
 constexpr int TI_THREADS = 64 + 32 * TI_NEPI;
 constexpr int TI_UR = 4;  // ring of unit indices handed from the producer to the MMA and epilogue warps
-constexpr int TI_PF = 2;  // tiled rows: tiles prefetched into L2 ahead of the ring
 constexpr size_t TI_SMEM = 1024 + (size_t)TI_STAGES * TI_STAGE_BYTES + 512;
 
 // order-preserving map of a float to an unsigned key
@@ -58,7 +57,7 @@ __global__ void __launch_bounds__(TI_THREADS, 1)
                   const int64_t *__restrict__ n_units_ptr, int K, const float *__restrict__ xnorm,
                   const int64_t *__restrict__ aslot, int seg_mul, float *__restrict__ scores,
                   uint32_t *__restrict__ tmin4, int *__restrict__ err, unsigned long long *__restrict__ next_unit,
-                  long long wait_limit, int drill, int tiled, const uint8_t *__restrict__ xg) {
+                  long long wait_limit, int drill, int tiled) {
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
     uint64_t *bars = reinterpret_cast<uint64_t *>(smem + TI_STAGES * TI_STAGE_BYTES);
@@ -113,14 +112,6 @@ __global__ void __launch_bounds__(TI_THREADS, 1)
                 const uint32_t bytes = TI_A_BYTES + (uint32_t)nsel * TI_BK * 2;
                 const int ntile = (int)((un.r1 - un.r0 + TI_M - 1) / TI_M);
                 for (int t = 0; t < ntile && ok; ++t) {
-                    // tiled rows: keep the unit's next TI_PF tiles on their way into
-                    // L2 (each one contiguous block of nk x 16 KB), so that the
-                    // ring's loads find them there: DRAM latency hidden without
-                    // shared memory
-                    if (tiled && xg)
-                        for (int tp = (t == 0 ? 1 : t + TI_PF); tp <= t + TI_PF && tp < ntile; ++tp)
-                            bulk_prefetch_l2(xg + (((un.xrow >> 7) + tp) * nk) * (int64_t)(TI_M * TI_BK * 2),
-                                             (uint32_t)nk * (TI_M * TI_BK * 2));
                     for (int kb = 0; kb < nk; ++kb, ++it) {
                         const int s = it % TI_STAGES;
                         const uint32_t ph = (it / TI_STAGES) & 1;
@@ -275,8 +266,7 @@ int tc_ivf_launch(const TcIvfLaunch &a, cudaStream_t st) {
     tc_ivf_kernel<<<a.grid, TI_THREADS, TI_SMEM, st>>>(mx, m32, m64, m128, a.units, a.n_units, a.K, a.xnorm,
                                                         a.aslot, a.seg_mul, a.scores, a.tmin4, a.err, a.next_unit,
                                                         a.wait_limit > 0 ? a.wait_limit : TC_TIMEOUT_CYCLES, a.drill,
-                                                        a.tiled,
-                                                        reinterpret_cast<const uint8_t *>(a.X));
+                                                        a.tiled);
     GN_CUDA_TRY(cudaGetLastError());
     return GN_OK;
 }
