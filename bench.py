@@ -55,6 +55,9 @@ NPROBES = [1, 2, 4, 6, 8, 12, 16, 20, 24, 28, 32, 40, 48, 64]
 # that the held-out evaluation queries stay at or above 0.95
 CAL_TARGET = 0.955
 PROB_THRESHOLDS = [0.5, 0.4, 0.3, 0.25, 0.22, 0.2, 0.19, 0.18, 0.17, 0.16, 0.15, 0.12, 0.1, 0.05, 0.02]
+# concurrent search contexts: the index and LANES - 1 forks of it (shared lists,
+# own scratch), one stream each; a step's batches go to the lanes round-robin
+LANES = 4
 
 
 # ── environment helpers ───────────────────────────────────────────────────
@@ -235,35 +238,62 @@ def bench_ivf(args, dist, peaks, peak_src):
     stream = torch.cuda.current_stream(dev)
     d_q = torch.from_numpy(stepq).to(dev)
     nmax = max(batches)
-    d_idx = torch.empty((nmax, K), dtype=torch.int64, device=dev)
-    d_dist = torch.empty((nmax, K), dtype=torch.float32, device=dev)
-    d_cnt = torch.empty((nmax,), dtype=torch.int64, device=dev)
+    lanes = [ix] + [ix.fork() for _ in range(LANES - 1)]
+    lane_streams = [torch.cuda.Stream(dev) for _ in lanes]
+    lane_done = [torch.cuda.Event() for _ in lanes]
+    step_start = torch.cuda.Event()
+    lane_out = [(torch.empty((nmax, K), dtype=torch.int64, device=dev),
+                 torch.empty((nmax, K), dtype=torch.float32, device=dev),
+                 torch.empty((nmax,), dtype=torch.int64, device=dev)) for _ in lanes]
+    d_idx, d_dist, d_cnt = lane_out[0]
     offs = np.concatenate([[0], np.cumsum(batches)])
 
-    def run_step(timing=False):
+    def run_step(timing=False, nl=LANES):
+        """One pass over the step's batches: batch b on lane b % nl (nl = 1:
+        the index alone, in order on the current stream)."""
         kms = 0.0
+        if nl > 1:
+            step_start.record(stream)
+            for s in lane_streams[:nl]:
+                s.wait_event(step_start)
         for b, (o, nb) in enumerate(zip(offs[:-1], batches)):
             qp = ctypes.c_void_p(d_q.data_ptr() + int(o) * IVF_D * 4)
-            _lib.check(lib.gn_ivfl2_search_knn_device(ix._h.h, qp, int(nb), K, vp(d_idx), vp(d_dist), vp(d_cnt),
-                                                      ctypes.c_void_p(stream.cuda_stream)))
+            ln = b % nl
+            st = stream if nl == 1 else lane_streams[ln]
+            oi, od, oc = lane_out[ln]
+            _lib.check(lib.gn_ivfl2_search_knn_device(lanes[ln]._h.h, qp, int(nb), K, vp(oi), vp(od), vp(oc),
+                                                      ctypes.c_void_p(st.cuda_stream)))
             if timing:
                 t = ctypes.c_float()
                 _lib.check(lib.gn_timing_last(ctypes.byref(t), None, 0))
                 kms += t.value
+        if nl > 1:
+            for s, e in zip(lane_streams[:nl], lane_done):
+                e.record(s)
+                stream.wait_event(e)
         return kms
 
     tuning = {}
 
-    def timed(engine, nprobe, steps, warmup, thr=None, graphs=True, profile=False):
-        ix.set_engine(engine)
-        ix.n_probe = nprobe
-        ix.set_prober(prober if thr is not None else None, thr if thr is not None else 0.5)
-        if engine == "tc":  # launch choices per batch-size bucket, timed on 4096 sample queries
-            tuning[(nprobe, thr)] = ix.autotune(tune_q, K).tolist()
-        # one captured CUDA graph per batch size, captured during the warm-up
-        ix.enable_graphs(nmax if graphs else 0, K)
+    def configure(engine, nprobe, thr=None, graphs=True):
+        """The same settings on the index and its forks (each lane has its own)."""
+        for x in lanes:
+            x.set_engine(engine)
+            x.n_probe = nprobe
+            x.set_prober(prober if thr is not None else None, thr if thr is not None else 0.5)
+        if engine == "tc":  # launch choices per batch-size bucket, timed once on 4096 sample queries
+            if (nprobe, thr) not in tuning:
+                tuning[(nprobe, thr)] = ix.autotune(tune_q, K).tolist()
+            for x in lanes:
+                x.tuning = tuning[(nprobe, thr)]
+        # one captured CUDA graph per batch size and lane, captured during the warm-up
+        for x in lanes:
+            x.enable_graphs(nmax if graphs else 0, K)
+
+    def timed(engine, nprobe, steps, warmup, thr=None, graphs=True, profile=False, nl=LANES):
+        configure(engine, nprobe, thr, graphs)
         for _ in range(warmup):
-            run_step()
+            run_step(nl=nl)
         torch.cuda.synchronize()
         dist.barrier()
         torch.cuda.synchronize()
@@ -273,7 +303,7 @@ def bench_ivf(args, dist, peaks, peak_src):
             torch.cuda.profiler.start()
         for s in range(steps):
             ev0[s].record(stream)
-            run_step()
+            run_step(nl=nl)
             ev1[s].record(stream)
         torch.cuda.synchronize()
         if profile:
@@ -281,17 +311,21 @@ def bench_ivf(args, dist, peaks, peak_src):
         dist.barrier()
         ms = [a.elapsed_time(b) for a, b in zip(ev0, ev1)]
         tot = dist.max(sum(ms) / 1e3)
-        # kernel timing in a separate pass (the event bracket adds a host wait)
+        # kernel timing in a separate pass, one lane (the event bracket adds a host wait)
         lib.gn_timing_enable(1)
-        kern = statistics.mean(run_step(timing=True) for _ in range(2))
+        kern = statistics.mean(run_step(timing=True, nl=1) for _ in range(2))
         lib.gn_timing_enable(0)
         idx, _, _ = ix.search_knn_arrays(ev, K)
         rec = recall_at(idx, gt_ev)
+        # every lane returns the index's results
+        for x in lanes[1:]:
+            if not np.array_equal(x.search_knn_arrays(ev[:200], K)[0], idx[:200]):
+                raise RuntimeError("a fork of the index returned other results than the index")
         lists = float(ix.last_lists_probed(len(ev)).mean()) if thr is not None else float(nprobe)
         ginfo = ix.graph_info()
         return {"qps": STEP_QUERIES * steps * dist.ws / tot, "ms_per_step": statistics.mean(ms), "steps_ms": ms,
                 "kernel_ms_per_step": kern, "recall_eval": rec, "mean_lists_probed": lists, "cuda_graphs": graphs,
-                "graphs_cached": ginfo["graphs"], "graph_capture_failures": ginfo["capture_failures"]}
+                "graphs_cached": ginfo["graphs"], "graph_capture_failures": ginfo["capture_failures"], "lanes": nl}
 
     plain_p, plain_cal = calibrate("fp32")
     tcfix_p, tcfix_cal = calibrate("tc")
@@ -346,11 +380,11 @@ def bench_ivf(args, dist, peaks, peak_src):
     tcfix = timed("tc", tcfix_p, max(2, args.steps // 2), args.warmup)
     tuned = timed("tc", tcfix_p, args.steps, args.warmup, thr=thr_sel, profile=True)
     tuned_ng = timed("tc", tcfix_p, max(2, args.steps // 2), args.warmup, thr=thr_sel, graphs=False)
+    tuned_1 = timed("tc", tcfix_p, max(2, args.steps // 2), args.warmup, thr=thr_sel, nl=1)
     clocks = sampler.stop()
 
     # work accounting for the roofline: one full-size batch of the tuned engine
-    ix.set_engine("tc")
-    ix.set_prober(prober, thr_sel)
+    # (the settings of the last timed arm)
     nb = min(4096, len(stepq))
     _lib.check(lib.gn_ivfl2_search_knn_device(ix._h.h, vp(d_q), nb, K, vp(d_idx), vp(d_dist), vp(d_cnt),
                                               ctypes.c_void_p(stream.cuda_stream)))
@@ -408,35 +442,47 @@ def bench_ivf(args, dist, peaks, peak_src):
     ix.set_engine("tc")
     ix.n_probe = tcfix_p
 
-    # e2e through the C ABI with pinned host buffers
+    # e2e through the C ABI with pinned host buffers: one host thread per lane,
+    # each calling the blocking host entry point (queries in, results out) on
+    # its own fork for batches b = lane, lane + LANES, ...
+    from concurrent.futures import ThreadPoolExecutor
+
     h_q = torch.from_numpy(stepq).pin_memory()
-    h_idx = torch.empty((nmax, K), dtype=torch.int64).pin_memory()
-    h_dist = torch.empty((nmax, K), dtype=torch.float32).pin_memory()
-    h_cnt = torch.empty((nmax,), dtype=torch.int64).pin_memory()
+    h_out = [(torch.empty((nmax, K), dtype=torch.int64).pin_memory(),
+              torch.empty((nmax, K), dtype=torch.float32).pin_memory(),
+              torch.empty((nmax,), dtype=torch.int64).pin_memory()) for _ in lanes]
+
+    def e2e_lane(ln):
+        hi, hd, hc = h_out[ln]
+        for b in range(ln, len(batches), LANES):
+            qp = ctypes.c_void_p(h_q.data_ptr() + int(offs[b]) * IVF_D * 4)
+            _lib.check(lib.gn_ivfl2_search_knn(lanes[ln]._h.h, qp, int(batches[b]), K, vp(hi), vp(hd), vp(hc)))
+
+    configure("tc", tcfix_p, thr_sel, graphs=True)
+    pool = ThreadPoolExecutor(LANES)
 
     def e2e_step():
-        for o, nb_ in zip(offs[:-1], batches):
-            qp = ctypes.c_void_p(h_q.data_ptr() + int(o) * IVF_D * 4)
-            _lib.check(lib.gn_ivfl2_search_knn(ix._h.h, qp, int(nb_), K, vp(h_idx), vp(h_dist), vp(h_cnt)))
+        list(pool.map(e2e_lane, range(LANES)))
 
-    ix.set_engine("tc")
-    ix.set_prober(prober, thr_sel)
-    ix.enable_graphs(nmax, K)
     e2e_step()
     dist.barrier()
     t0 = time.perf_counter()
     for _ in range(args.steps):
         e2e_step()
     e2e_s = dist.max(time.perf_counter() - t0)
+    pool.shutdown()
     e2e = {"value": STEP_QUERIES * args.steps * dist.ws / e2e_s, "unit": "queries/s",
-           "h2d_bytes_per_step": int(stepq.nbytes), "d2h_bytes_per_step": int(STEP_QUERIES * K * (8 + 4) + STEP_QUERIES * 8)}
+           "h2d_bytes_per_step": int(stepq.nbytes), "d2h_bytes_per_step": int(STEP_QUERIES * K * (8 + 4) + STEP_QUERIES * 8),
+           "lanes": f"{LANES} host threads, one fork each, blocking host entry point"}
     # kernels per tuned batch: BF16 queries, coarse units, coarse scan, coarse+MLP, planning (one kernel up
     # to 16,384 (query, list) pairs with 64 probe candidates per query, else five), Qb + units (one
     # kernel), scan, select; the launch list of one step in profiles/ shows the same 8 / 12
     launches_per_step = sum(8 if nb_ * 64 <= 16384 else 12 for nb_ in batches)
     cent, offs_l, ids = ix.export()
-    ix.enable_graphs(0, 0)
-    return {"tuned": tuned, "plain": plain, "tc_fixed": tcfix, "tuned_no_graphs": tuned_ng,
+    for x in lanes:
+        x.enable_graphs(0, 0)
+    del lanes[1:]
+    return {"tuned": tuned, "plain": plain, "tc_fixed": tcfix, "tuned_no_graphs": tuned_ng, "tuned_one_lane": tuned_1,
             "tuned_nprobe": tcfix_p, "plain_nprobe": plain_p,
             "tuned_threshold": thr_sel,
             "prober": {"train_queries": N_TRAIN, "epochs": 4, "losses": [float(x) for x in losses],
@@ -1064,7 +1110,9 @@ def main():
                        "plain_qps": p["qps"], "tc_fixed_qps": ivf["tc_fixed"]["qps"],
                        "mean_lists_probed": t["mean_lists_probed"], "prob_threshold": ivf["tuned_threshold"],
                        "plain_nprobe": ivf["plain_nprobe"], "tc_fixed_nprobe": ivf["tuned_nprobe"],
-                       "l2": "index data (3 GB) exceeds L2; no flush", "parallelism": f"replicas x{ws}"},
+                       "l2": "index data (3 GB) exceeds L2; no flush", "parallelism": f"replicas x{ws}",
+                       "lanes": LANES, "lanes_note": "batches round-robin over the index and its forks, one stream each",
+                       "tuned_one_lane_qps": ivf["tuned_one_lane"]["qps"]},
             "recall_at_10": {"tuned": t["recall_eval"], "plain": p["recall_eval"],
                              "calibration": ivf["calibration"]},
             "plain": {"value": p["qps"], "ms_per_step": p["ms_per_step"], "nprobe": ivf["plain_nprobe"],

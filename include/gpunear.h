@@ -152,6 +152,15 @@ int gn_ivfl2_set_assigned(gn_index *ix, const float *data, int64_t n, int64_t d,
                           int32_t n_centroids, const int32_t *labels);
 int gn_ivfl2_search_knn(gn_index *ix, const float *queries, int64_t nq, int64_t k, int64_t *out_idx,
                         float *out_dist, int64_t *out_cnt);
+/* Concurrent search contexts (no reference counterpart; results unchanged):
+ * a fork views the parent's lists (centroids, CSR offsets, rows, ids; nothing
+ * is copied) and owns its scratch, stream, error word and captured graphs, so
+ * searches on the parent and its forks may run at the same time, each on its
+ * own stream.  Settings (n_probe, engine, shortlist, prober, tuning) start as
+ * the parent's.  While forks live, set / set_assigned on the parent fail with
+ * GN_ERR_INVALID; gn_index_destroy of the parent defers its release to the
+ * last fork's.  Forks of forks are refused. */
+int gn_ivfl2_fork(gn_index *parent, gn_index **out);
 /* device variant: queries [nq x d] row-major on the device; results written
  * to device buffers in stream order (no synchronisation).  Searches of one
  * index share its scratch: issue them on one stream, or order them (with

@@ -60,6 +60,7 @@ SIGNATURES = {
     "gn_ivfl2_create": [I32, I32, PP],
     "gn_ivfl2_set": [P, P, I64, I64],
     "gn_ivfl2_set_assigned": [P, P, I64, I64, P, I32, P],
+    "gn_ivfl2_fork": [P, PP],
     "gn_ivfl2_search_knn": [P, P, I64, I64, P, P, P],
     "gn_ivfl2_search_knn_device": [P, P, I64, I64, P, P, P, P],
     "gn_ivfl2_enable_graphs": [P, I64, I32],

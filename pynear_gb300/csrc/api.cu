@@ -35,6 +35,7 @@ uint64_t dbuf_generation() { return g_dbuf_gen.load(std::memory_order_relaxed); 
 
 int DBuf::ensure(size_t bytes) {
     if (bytes <= cap && p) return GN_OK;
+    if (!own) return fail(GN_ERR_INVALID, "a buffer shared with a parent index cannot be reallocated");
     g_dbuf_gen.fetch_add(1, std::memory_order_relaxed);  // device pointers held elsewhere may go stale
     release();
     size_t want = std::max<size_t>(bytes, 256);
@@ -49,9 +50,23 @@ int DBuf::ensure(size_t bytes) {
     return GN_OK;
 }
 void DBuf::release() {
-    if (p) cudaFree(p);
+    if (p && own) cudaFree(p);
     p = nullptr;
     cap = 0;
+    own = true;
+}
+
+static std::mutex g_fork_mu;
+
+void fork_attach(gn_index *child, gn_index *parent) {
+    std::lock_guard<std::mutex> g(g_fork_mu);
+    child->fork_parent = parent;
+    parent->fork_count++;
+}
+
+bool has_forks(gn_index *ix) {
+    std::lock_guard<std::mutex> g(g_fork_mu);
+    return ix->fork_count > 0;
 }
 
 int HBuf::ensure(size_t bytes) {
@@ -140,7 +155,19 @@ int gn_flat_create(int metric, gn_index **out) {
 }
 
 int gn_index_destroy(gn_index *ix) {
-    delete ix;
+    if (!ix) return GN_OK;
+    gn_index *parent_done = nullptr;
+    {
+        std::lock_guard<std::mutex> g(g_fork_mu);
+        if (ix->fork_count > 0) {  // forks still read its lists: deleted with the last fork
+            ix->destroy_pending = true;
+            return GN_OK;
+        }
+        if (gn_index *p = ix->fork_parent)
+            if (--p->fork_count == 0 && p->destroy_pending) parent_done = p;
+    }
+    delete ix;  // a fork's views of the parent's lists are not freed
+    delete parent_done;
     return GN_OK;
 }
 

@@ -8,12 +8,21 @@
 
 namespace gn {
 
-// Growable device allocation owned by an index (freed in the destructor).
+// Growable device allocation owned by an index (freed in the destructor), or
+// a view of another index's allocation (a fork's shared list data: never
+// freed or grown through the view).
 struct DBuf {
     void *p = nullptr;
     size_t cap = 0;
+    bool own = true;
     int ensure(size_t bytes);
     void release();
+    void view(const DBuf &o) {
+        release();
+        p = o.p;
+        cap = o.cap;
+        own = false;
+    }
     template <typename T>
     T *as() const { return reinterpret_cast<T *>(p); }
     ~DBuf() { release(); }
@@ -58,12 +67,23 @@ struct gn_index {
     gn::IvfBinState *ivfbin = nullptr;
     void *ext = nullptr;                  // other engines' state
     void (*ext_free)(void *) = nullptr;
+    // forks (concurrent search contexts over one index's lists): a fork points
+    // at its parent; a parent counts its live forks and, when destroyed while
+    // some are alive, is deleted with the last of them (guarded by a global
+    // mutex in api.cu)
+    gn_index *fork_parent = nullptr;
+    int fork_count = 0;
+    bool destroy_pending = false;
     ~gn_index();
 };
 
 namespace gn {
 
 int make_stream(gn_index *ix);
+// Register a new fork of `parent` / ask whether an index has live forks
+// (under the fork mutex).
+void fork_attach(gn_index *child, gn_index *parent);
+bool has_forks(gn_index *ix);
 // Counter bumped whenever any DBuf (re)allocates: captured CUDA graphs that
 // hold device pointers compare it to know whether they are still valid.
 uint64_t dbuf_generation();

@@ -953,8 +953,16 @@ static int ivfl2_check(gn_index *ix) {
     return GN_OK;
 }
 
+// The lists of an index with live forks, or of a fork, stay as they are.
+static int ivfl2_check_rebuild(gn_index *ix) {
+    if (ix->fork_parent) return fail(GN_ERR_INVALID, "a fork shares its parent's lists: call set() on a new index");
+    if (has_forks(ix)) return fail(GN_ERR_INVALID, "the index has live forks that share its lists: destroy them first");
+    return GN_OK;
+}
+
 int gn_ivfl2_set(gn_index *ix, const float *data, int64_t n, int64_t d) {
     GN_TRY(ivfl2_check(ix));
+    GN_TRY(ivfl2_check_rebuild(ix));
     if (n <= 0 || d <= 0 || !data) return fail(GN_ERR_INVALID, "data must be a 2-D array of shape (N, D)");
     if (n >= 0x7fffffffLL) return fail(GN_ERR_UNSUPPORTED, "at most 2^31-2 rows");
     std::lock_guard<std::mutex> lk(ix->mu);
@@ -984,6 +992,7 @@ int gn_ivfl2_set(gn_index *ix, const float *data, int64_t n, int64_t d) {
 int gn_ivfl2_set_assigned(gn_index *ix, const float *data, int64_t n, int64_t d, const float *centroids,
                           int32_t n_centroids, const int32_t *labels) {
     GN_TRY(ivfl2_check(ix));
+    GN_TRY(ivfl2_check_rebuild(ix));
     if (n <= 0 || d <= 0 || !data || !centroids || !labels || n_centroids <= 0)
         return fail(GN_ERR_INVALID, "set_assigned: bad arguments");
     std::lock_guard<std::mutex> lk(ix->mu);
@@ -998,6 +1007,68 @@ int gn_ivfl2_set_assigned(gn_index *ix, const float *data, int64_t n, int64_t d,
     ix->n = n;
     ix->dim = d;
     return ivfl2_build_from_labels(ix, X.as<float>(), n, (int)d, dp, hc, n_centroids, lab, st);
+}
+
+// A fork: a second search context over the parent's lists.  It views the
+// parent's read-only data (centroids, CSR offsets, FP32 and tiled BF16 rows,
+// ids) and owns everything a search writes (scratch, error word, unit
+// counters, stream, captured graphs), so searches on the parent and its forks
+// run concurrently on different streams.  Settings (n_probe, engine,
+// shortlist, prober, tuning table) start as copies of the parent's and are
+// the fork's own from then on.
+int gn_ivfl2_fork(gn_index *parent, gn_index **out) {
+    GN_TRY(ivfl2_check(parent));
+    if (!out) return fail(GN_ERR_INVALID, "out is NULL");
+    if (parent->fork_parent) return fail(GN_ERR_INVALID, "fork the parent index, not a fork");
+    std::lock_guard<std::mutex> lk(parent->mu);
+    IvfL2State &P = *parent->ivfl2;
+    if (P.nc == 0) return fail(GN_ERR_EMPTY, "Index is empty — call set() first");
+    GN_TRY(make_stream(parent));
+    if (P.K == 0) GN_TRY(ivfl2_prepare_tc(parent, parent->stream));  // tiled BF16 rows, shared from here on
+    GN_CUDA_TRY(cudaStreamSynchronize(parent->stream));
+    gn_index *ix = new gn_index();
+    ix->kind = K_IVFL2;
+    ix->metric = parent->metric;
+    ix->n = parent->n;
+    ix->dim = parent->dim;
+    ix->ivfl2 = new IvfL2State();
+    IvfL2State &S = *ix->ivfl2;
+    S.nlist_req = P.nlist_req;
+    S.nprobe = P.nprobe;
+    S.d = P.d;
+    S.dp = P.dp;
+    S.nc = P.nc;
+    S.n = P.n;
+    S.h_off = P.h_off;
+    S.top_rows = P.top_rows;
+    S.rc = P.rc;
+    S.mode = P.mode;
+    S.shortlist = P.shortlist;
+    S.K = P.K;
+    S.x16_rows = P.x16_rows;
+    S.prober = P.prober;
+    S.prober_tau = P.prober_tau;
+    for (int b = 0; b < 7; ++b) S.tune[b] = P.tune[b];
+    S.cent.view(P.cent);
+    S.cnorm.view(P.cnorm);
+    S.list_off.view(P.list_off);
+    S.vecs.view(P.vecs);
+    S.vnorm.view(P.vnorm);
+    S.ids.view(P.ids);
+    S.x16.view(P.x16);
+    S.xoff.view(P.xoff);
+    S.c16.view(P.c16);
+    // the fork's own error word and unit counters
+    int rc = S.err.ensure(4);
+    if (rc == GN_OK) rc = S.sched.ensure(2 * sizeof(unsigned long long));
+    if (rc == GN_OK && cudaMemset(S.err.p, 0, 4) != cudaSuccess) rc = fail(GN_ERR_CUDA, "fork: clearing the error word");
+    if (rc != GN_OK) {
+        delete ix;
+        return rc;
+    }
+    fork_attach(ix, parent);
+    *out = ix;
+    return GN_OK;
 }
 
 int gn_ivfl2_search_knn_device(gn_index *ix, const float *d_queries, int64_t nq, int64_t k, int64_t *d_idx,

@@ -106,7 +106,7 @@ class IVFFlatL2Index:
     def autotune(self, sample_queries, k: int, reps: int = 3) -> np.ndarray:
         """Time the tensor-core engine's launch choices on sample queries for
         every batch-size bucket the sample reaches and keep the fastest; returns
-        the (7, 3) table of (rows per work unit, most blocks per query
+        the (7, 4) table of (rows per work unit, most blocks per query
         selection, selector threads, queries per list-scan work unit) per
         bucket.  Results are unchanged."""
         q = _f32_2d(sample_queries, "sample_queries")
@@ -143,6 +143,47 @@ class IVFFlatL2Index:
                   cent.shape[0], _lib.ptr(lab))
         self._built = arr.shape[0] > 0
         self._data = arr
+
+    def fork(self) -> "IVFFlatL2Index":
+        """A second search context over this index's lists.  It shares the
+        device data (centroids, lists, rows: nothing is copied) and owns its
+        scratch, stream and captured graphs, so searches on the index and on
+        its forks can run at the same time, each fork on its own stream.
+        n_probe, engine, prober and tuning start as this index's and are the
+        fork's own afterwards.  While forks are alive the index cannot be
+        rebuilt (set / set_assigned raise)."""
+        if not self._built:
+            raise RuntimeError("Index is empty — call set() first")
+        f = IVFFlatL2Index.__new__(IVFFlatL2Index)
+        f._n_clusters_req, f._n_probe = self._n_clusters_req, self._n_probe
+        f._h = _lib.Handle("gn_ivfl2_fork", self._h.h)
+        f._built, f._state, f._data = True, None, self._data
+        f._engine, f._shortlist = self._engine, self._shortlist
+        f._parent = self  # the lists' owner
+        if getattr(self, "_prober", None) is not None:
+            f._prober, f._prober_threshold = self._prober, self._prober_threshold
+        return f
+
+    def search_knn_device(self, queries, k: int, out_idx, out_dist, out_cnt, stream=None) -> None:
+        """Search device-resident queries (a contiguous float32 CUDA tensor
+        (nq, d)) into device tensors idx (nq, k) int64, dist (nq, k) float32
+        and count (nq,) int64, in the order of `stream` (a torch.cuda.Stream;
+        default: the current stream), without synchronising."""
+        import torch
+        if not self._built:
+            raise RuntimeError("Index is empty — call set() first")
+        if queries.dtype != torch.float32 or not queries.is_cuda or not queries.is_contiguous() or queries.dim() != 2:
+            raise ValueError("queries must be a contiguous 2-D float32 CUDA tensor")
+        nq, k = int(queries.shape[0]), int(k)
+        for t, dt, shape in ((out_idx, torch.int64, (nq, k)), (out_dist, torch.float32, (nq, k)),
+                             (out_cnt, torch.int64, (nq,))):
+            if t.dtype != dt or not t.is_cuda or not t.is_contiguous() or tuple(t.shape[:len(shape)]) != shape:
+                raise ValueError(f"output tensors must be contiguous CUDA tensors of shape {shape} and {dt}")
+        if stream is None:
+            stream = torch.cuda.current_stream(queries.device)
+        if nq:
+            _lib.call("gn_ivfl2_search_knn_device", self._h.h, queries.data_ptr(), nq, k, out_idx.data_ptr(),
+                      out_dist.data_ptr(), out_cnt.data_ptr(), stream.cuda_stream)
 
     def search_knn_arrays(self, queries, k: int):
         """(idx (nq,k) int64, dist (nq,k) float32, count (nq,) int64), nearest-first."""
