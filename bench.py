@@ -1059,16 +1059,138 @@ def run_reference(args):
             "e2e": {"value": v, "unit": "queries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
+# ── small profiling cases (one profiler region around exactly one call) ─────
+PROFILE_CASES = ("ivf_scan", "ivf_mlp", "tc_shortlist", "flat_l2_hbm", "hamming", "voronoi")
+
+
+def profile_case(name):
+    """One small case of one kernel for `ncu --profile-from-start off`: the
+    data are built, two warm-up calls run, then a profiler region opens around
+    exactly one call.  Sizes keep the inputs above L2 (129 MB) and the device
+    footprint to a few GB:
+      ivf_scan      400,000 x 512 Zipf mixture (820 centres), nlist 410,
+                    tensor-core engine, n_probe 11, one 4,096-query batch: the
+                    region launches the coarse scan (tc_ivf_kernel #1), the
+                    list scan (tc_ivf_kernel #2), the probe stage and select;
+      ivf_mlp       the same index and batch with a learned prober attached
+                    (untrained weights: the probe stage's fused MLP,
+                    coarse_probe_kernel<1>, costs the same whatever they are);
+      tc_shortlist  1,000,000 x 128 mixture, 2,048 queries, BF16, shortlist 40;
+      flat_l2_hbm   exact flat L2, 1,000,000 x 128 FP32, 8 queries;
+      hamming       exact Hamming, 1,000,000 x 512 bits, 10,000 queries;
+      voronoi       3840 x 2160 raster, 4,096 seeds.
+    Prints one JSON line with the call's CUDA-event time (outside the region)."""
+    import torch
+    import pynear_gb300 as gn
+    from pynear_gb300 import _lib, workloads as W
+
+    lib = _lib.load()
+    dev = torch.device("cuda", 0)
+    stream = torch.cuda.current_stream(dev)
+    info = {"case": name}
+    if name in ("ivf_scan", "ivf_mlp"):
+        db, q, _, _ = W.gaussian_mixture(n=400_000, d=512, n_centres=820, sigma=0.3, zipf_s=1.1, nq=4096, seed=3)
+        ix = gn.IVFFlatL2Index(n_clusters=410, n_probe=11, engine="tc")
+        ix.set(db)
+        if name == "ivf_mlp":
+            ix.set_prober(gn.LearnedProber(ix, seed=1), 0.5)
+        d_q = torch.from_numpy(q).to(dev)
+        o = (torch.empty((len(q), K), dtype=torch.int64, device=dev),
+             torch.empty((len(q), K), dtype=torch.float32, device=dev),
+             torch.empty((len(q),), dtype=torch.int64, device=dev))
+
+        def call():
+            _lib.check(lib.gn_ivfl2_search_knn_device(ix._h.h, vp(d_q), len(q), K, vp(o[0]), vp(o[1]), vp(o[2]),
+                                                      ctypes.c_void_p(stream.cuda_stream)))
+    elif name == "tc_shortlist":
+        db, q, _, _ = W.gaussian_mixture(n=1_000_000, d=128, n_centres=1024, sigma=0.3, zipf_s=0, nq=2048, seed=11)
+        ix = gn.FlatL2TCIndex(shortlist=40)
+        ix.set(db)
+        d_q = torch.from_numpy(q).to(dev)
+        o = (torch.empty((len(q), K), dtype=torch.int64, device=dev),
+             torch.empty((len(q), K), dtype=torch.float32, device=dev))
+
+        def call():
+            _lib.check(lib.gn_tcflat_search_knn_device(ix._h.h, vp(d_q), len(q), K, vp(o[0]), vp(o[1]),
+                                                       ctypes.c_void_p(stream.cuda_stream)))
+    elif name == "flat_l2_hbm":
+        rng = np.random.default_rng(17)
+        db = rng.standard_normal((1_000_000, 128), dtype=np.float32)
+        q = rng.standard_normal((8, 128), dtype=np.float32)
+        ix = gn.FlatL2Index()
+        ix.set(db)
+        d_q = torch.from_numpy(q).to(dev)
+        o = (torch.empty((len(q), K), dtype=torch.int64, device=dev),
+             torch.empty((len(q), K), dtype=torch.float32, device=dev))
+
+        def call():
+            _lib.check(lib.gn_flat_search_knn_device(ix._h.h, vp(d_q), len(q), K, vp(o[0]), vp(o[1]),
+                                                     ctypes.c_void_p(stream.cuda_stream)))
+    elif name == "hamming":
+        data, q, _ = W.hamming_flips(n=1_000_000, nbytes=64, nq=10_000, flips=24, seed=5)
+        ix = gn.FlatHammingIndex()
+        ix.set(data)
+        d_q = torch.from_numpy(q).to(dev)
+        o = (torch.empty((len(q), K), dtype=torch.int64, device=dev),
+             torch.empty((len(q), K), dtype=torch.int64, device=dev))
+
+        def call():
+            _lib.check(lib.gn_flat_search_knn_device(ix._h.h, vp(d_q), len(q), K, vp(o[0]), vp(o[1]),
+                                                     ctypes.c_void_p(stream.cuda_stream)))
+    elif name == "voronoi":
+        w, h = 3840, 2160
+        xs, ys = gn.voronoi.grid_axes(w, h)
+        d_xs, d_ys = torch.from_numpy(xs).to(dev), torch.from_numpy(ys).to(dev)
+        seeds = np.random.default_rng(4096).random((4096, 2), dtype=np.float32)
+        d_s = torch.from_numpy(seeds).to(dev)
+
+        def call():
+            gn.voronoi_raster_device(d_s, d_xs, d_ys, stream=stream)
+    else:
+        raise SystemExit(f"unknown profile case {name!r}; one of {', '.join(PROFILE_CASES)}")
+    for _ in range(2):
+        call()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    call()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    info["call_ms"] = e0.elapsed_time(e1)
+    torch.cuda.profiler.start()
+    call()
+    torch.cuda.synchronize()
+    torch.cuda.profiler.stop()
+    if name in ("ivf_scan", "ivf_mlp"):
+        w = np.zeros(4, np.int64)
+        _lib.check(lib.gn_ivfl2_last_work(ix._h.h, w.ctypes.data_as(ctypes.c_void_p)))
+        info.update(pairs=int(w[0]), scored_rows=int(w[1]), distinct_list_rows=int(w[2]), units=int(w[3]),
+                    bytes_alg=int(w[2]) * (512 * 2 + 4))
+    print(json.dumps(info))
+
+
 def main():
+    global LANES
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gpunear", choices=["gpunear", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--lanes", type=int, default=4,
+                    help="concurrent search contexts (the index and lanes - 1 forks, one stream each)")
+    ap.add_argument("--profile-case", choices=PROFILE_CASES,
+                    help="run one small case of one kernel inside a profiler region (for ncu) and exit")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    LANES = max(1, args.lanes)
     ws, rank, _ = dist_env()
+
+    if args.profile_case:
+        import __graft_entry__
+        __graft_entry__.build()
+        profile_case(args.profile_case)
+        return
 
     if args.impl == "reference":
         if rank == 0:

@@ -1058,6 +1058,8 @@ int gn_ivfl2_fork(gn_index *parent, gn_index **out) {
     S.x16.view(P.x16);
     S.xoff.view(P.xoff);
     S.c16.view(P.c16);
+    S.rho.view(P.rho);
+    S.xmax = P.xmax;
     // the fork's own error word and unit counters
     int rc = S.err.ensure(4);
     if (rc == GN_OK) rc = S.sched.ensure(2 * sizeof(unsigned long long));

@@ -7,10 +7,12 @@
 
 namespace gn {
 
+constexpr int IVF_RHO = 64;  // per list: radii of its rows nearest the centroid kept (>= the largest shortlist)
+
 // Per-batch scratch of an IVF search (device resident, reused).
 struct IvfScratch {
     DBuf q, qn, probes, probes64, pdist, bcnt, boff, bucket, fill, slot_rel, qcount, qslot, item_off, counter, part,
-        cpart, nprobed;
+        cpart, nprobed, qbound;  // qbound: per query, the ordered score bound of the tensor-core list scan
 };
 
 // Float IVF (forest.py IVFFlatL2Index semantics, squared L2).
@@ -36,7 +38,12 @@ struct IvfL2State {
                                  // contiguous, so one TMA box is one contiguous block
     DBuf xoff;                   // int64 nc + 1: padded start row of each list in x16
     int64_t x16_rows = 0;        // padded rows
-    DBuf qb, aslot, units, nunits, err, scores;
+    DBuf qb, aslot, abound, units, nunits, err, scores;
+    // score bound of the tensor-core list scan: per list, the distances |x - c|
+    // of its 64 rows nearest the centroid (ascending, slightly rounded up;
+    // +inf past the list's size), and the largest row norm of the index
+    DBuf rho;
+    float xmax = 0.f;
     DBuf sel_part, sel_done;     // split selection: partial best-S lists, per-query arrival counters
     DBuf sched;                  // unit counters of the tensor-core scans (coarse, lists)
     DBuf tmin;                   // per (score slot, 32-row quarter): minimum ordered score

@@ -78,12 +78,13 @@ __device__ void tc_units_body(int64_t i, const int64_t *__restrict__ item_off, i
 }
 
 // One launch for both: blocks [0, qb_blocks) fill Qb — row pos = the BF16 row
-// of the query of the pair bucket[pos], warp per row — the rest build the
-// work units.
+// of the query of the pair bucket[pos], warp per row, with the pair's slot
+// base and its query's score bound — the rest build the work units.
 __global__ void qb_units_kernel(const uint4 *__restrict__ q16, int K8, int np, const int64_t *__restrict__ bucket,
                                 const int64_t *__restrict__ boff, int nc, const int64_t *__restrict__ qslot,
                                 const int64_t *__restrict__ slot_rel, uint4 *__restrict__ qb,
-                                int64_t *__restrict__ aslot, int64_t max_pairs, unsigned qb_blocks,
+                                int64_t *__restrict__ aslot, const uint32_t *__restrict__ qbound,
+                                uint32_t *__restrict__ abound, int64_t max_pairs, unsigned qb_blocks,
                                 const int64_t *__restrict__ item_off, const int64_t *__restrict__ list_off,
                                 const int64_t *__restrict__ xoff, int rc, int qch, int64_t max_units,
                                 TcUnit *__restrict__ units, int64_t *__restrict__ n_units) {
@@ -94,7 +95,10 @@ __global__ void qb_units_kernel(const uint4 *__restrict__ q16, int K8, int np, c
         const int64_t pair = bucket[pos];
         const int64_t q = pair / np;
         for (int j = lane; j < K8; j += 32) qb[pos * K8 + j] = q16[q * K8 + j];
-        if (lane == 0) aslot[pos] = qslot[q] + slot_rel[pair];
+        if (lane == 0) {
+            aslot[pos] = qslot[q] + slot_rel[pair];
+            abound[pos] = qbound[q];
+        }
         return;
     }
     const int64_t i = (int64_t)(blockIdx.x - qb_blocks) * blockDim.x + threadIdx.x;
@@ -325,7 +329,8 @@ __device__ uint32_t block_kth_u32(const uint32_t *v, int n, int kth, int *hist, 
 // so ties go to the lower row.
 //   threshold  tau = the S-th smallest quarter minimum of the block's slots
 //              (radix select): S distinct rows score <= tau, so tau bounds the
-//              query's S-th best score;
+//              query's S-th best score; tau is capped by the query's bound
+//              from the probe stage, above which the scan stored no quarter;
 //   sweep      warps take 8 slots at a time (lane l: quarter l % 4 of slot
 //              l / 4) and load only the 32-row quarters whose minimum is
 //              <= tau (one coalesced 128-byte load each, four in flight) —
@@ -338,7 +343,8 @@ __device__ uint32_t block_kth_u32(const uint32_t *v, int n, int kth, int *hist, 
 //              lower original index.
 template <int NT>
 __global__ void __launch_bounds__(NT, 1024 / NT) ivf_tc_select_kernel(
-    const float *__restrict__ scores, const uint4 *__restrict__ tmin4, const int32_t *__restrict__ probes, int np,
+    const float *__restrict__ scores, const uint4 *__restrict__ tmin4, const uint32_t *__restrict__ qbound,
+    const int32_t *__restrict__ probes, int np,
     const int64_t *__restrict__ qseg, const int64_t *__restrict__ seg_rel, const int64_t *__restrict__ list_off,
     int S, const float *__restrict__ Q, const float *__restrict__ X, int d, int dp, const int32_t *__restrict__ ids,
     int64_t nq, int k, int B, uint64_t *__restrict__ part, int *__restrict__ done, int64_t *__restrict__ out_idx,
@@ -409,7 +415,8 @@ __global__ void __launch_bounds__(NT, 1024 / NT) ivf_tc_select_kernel(
                 tm[4 * i + 3] = m.w;
             }
             __syncthreads();
-            tau = block_kth_u32<NT>(tm, 4 * ns, S, hist, sh);
+            // and never above the query's bound: quarters above it were not stored
+            tau = min(block_kth_u32<NT>(tm, 4 * ns, S, hist, sh), qbound[q]);
             wthr = tau == 0xffffffffu ? KEY_EMPTY : make_key(tau, 0xffffffffu);
         }
         int p = 0;  // probe of this lane's slot (monotone over the sweep)
@@ -557,7 +564,7 @@ __global__ void __launch_bounds__(NT, 1024 / NT) ivf_tc_select_kernel(
 // output as ivf_tc_select_kernel.
 //   threshold  tau = the S-th smallest quarter minimum of the query's first 64
 //              slots (a bitwise select over the warp's 256 values): S distinct
-//              rows score <= tau;
+//              rows score <= tau; capped by the query's bound;
 //   sweep      the block kernel's warp loop over all the query's slots: 8
 //              slots a step, only quarters whose minimum is <= tau are read,
 //              their scores <= the warp threshold buffered as keys;
@@ -569,7 +576,8 @@ __global__ void __launch_bounds__(NT, 1024 / NT) ivf_tc_select_kernel(
 constexpr int SELW_WARPS = 4;
 
 __global__ void __launch_bounds__(32 * SELW_WARPS) ivf_tc_select_warp_kernel(
-    const float *__restrict__ scores, const uint4 *__restrict__ tmin4, const int32_t *__restrict__ probes, int np,
+    const float *__restrict__ scores, const uint4 *__restrict__ tmin4, const uint32_t *__restrict__ qbound,
+    const int32_t *__restrict__ probes, int np,
     const int64_t *__restrict__ qseg, const int64_t *__restrict__ seg_rel, const int64_t *__restrict__ list_off,
     int S, const float *__restrict__ Q, const float *__restrict__ X, int d, int dp, const int32_t *__restrict__ ids,
     int64_t nq, int k, int64_t *__restrict__ out_idx, float *__restrict__ out_dist, int64_t *__restrict__ out_cnt) {
@@ -646,6 +654,7 @@ __global__ void __launch_bounds__(32 * SELW_WARPS) ivf_tc_select_warp_kernel(
             if (cnt < S) tau |= 1u << b;
         }
     }
+    tau = min(tau, qbound[q]);  // quarters above the query's bound were not stored
     uint64_t wthr = tau == 0xffffffffu ? KEY_EMPTY : make_key(tau, 0xffffffffu);
     int wn = 0;
     int p = 0;  // probe of this lane's slot (monotone over the sweep)
@@ -771,6 +780,39 @@ __global__ void coarse_units_kernel(int64_t nq, int nc, TcUnit *__restrict__ uni
 
 constexpr int PROBE_MAX_D = 2048;  // query row staged in shared memory
 
+// The query's score bound for the list scan, from b = this thread's probed
+// candidate list's distance bound (+inf for threads without one): with D the
+// smallest b, at least `shortlist` scored rows x have |q - x|^2 <= D, so the
+// shortlist-th smallest exact score |x|^2 - 2 q.x is at most D - |q|^2.  The
+// scan's BF16 score differs from the exact one by at most
+// 2 |q.x - acc| + rounding <= 2 (2^-7 + 2^-16 + 2^-9 (1 + 2^-8)^2) |q| |x| + ...
+// (both operands rounded to 8 significant bits; 2^-9 of sum |q_i x_i| allowed
+// for the tensor core's accumulation, far above FP32's), so the bound adds
+// 0.03 |q| xmax + 2^-12 (xmax + |q|)^2 and rounds every other term outwards.
+// Block-wide (all threads call it); thread 0 writes the ordered bound, or all
+// ones when there is none.
+__device__ __forceinline__ void write_probe_bound(float b, const float *sqr, int d, float xmax,
+                                                  uint32_t *__restrict__ qbound, int64_t q, float *red) {
+    const int j = threadIdx.x, lane = j & 31, warp = j >> 5;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) b = fminf(b, __shfl_xor_sync(0xffffffffu, b, o));
+    if (warp == 2) {
+        float s = 0.f;
+        for (int t = lane; t < d; t += 32) s = fmaf(sqr[t], sqr[t], s);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if (lane == 0) red[2] = s;
+    }
+    if (lane == 0 && warp < 2) red[warp] = b;
+    __syncthreads();
+    if (j == 0) {
+        const float D = fminf(red[0], red[1]), qn = red[2], qa = sqrtf(qn);
+        const float B = D * (1.f + 1.f / 1024.f) - qn * (1.f - 1.f / 1024.f) + 0.03f * qa * xmax +
+                        (xmax + qa) * (xmax + qa) * (1.f / 4096.f);
+        qbound[q] = (B < INFINITY && B == B) ? f2ord(B) : 0xffffffffu;
+    }
+}
+
 // Per query (block of 256 threads): the 64 best centroids by BF16 score, their
 // exact squared distances (FP32), sorted nearest first; then either the first
 // np of them (fixed probing) or the learned prober's choice (MLP fused here).
@@ -780,11 +822,13 @@ __global__ void __launch_bounds__(256) coarse_probe_kernel(const float *__restri
                                                            const float *__restrict__ C, int64_t nq, int np,
                                                            ProberWeights w, float logit_tau,
                                                            int32_t *__restrict__ probes,
-                                                           int32_t *__restrict__ nprobed) {
+                                                           int32_t *__restrict__ nprobed,
+                                                           const float *__restrict__ rho, int shortlist, float xmax,
+                                                           uint32_t *__restrict__ qbound) {
     constexpr int NC = PROBER_CAND, H = PROBER_HIDDEN;
     static_assert(H == 256 && NC == 64, "warp-per-row MLP layout: 32 lanes x 8 weights, 8 warps x 8 candidates");
     __shared__ int32_t sc[NC];
-    __shared__ float sd[NC], sf[NC], sz[NC];
+    __shared__ float sd[NC], sf[NC], sz[NC], sb[NC], sred[4];
     __shared__ __align__(16) float sh1[H], sh2[H];
     __shared__ int s_cnt0;
     __shared__ __align__(16) float sqr[PROBE_MAX_D];
@@ -872,10 +916,23 @@ __global__ void __launch_bounds__(256) coarse_probe_kernel(const float *__restri
         const float d1 = __uint_as_float(key_dist(skeys[0]));
         sc[j] = e ? -1 : (int32_t)key_idx(k);
         sf[j] = e ? 0.f : fmaxf(0.f, 1.f - (__uint_as_float(key_dist(k)) - d1) / fmaxf(d1, 1e-12f));
+        // bound on the squared distance of the query's shortlist-th nearest row if
+        // this list is probed: its `shortlist` rows nearest the centroid lie within
+        // rho of it, hence within |q - c| + rho of the query
+        float b = INFINITY;
+        if (qbound && !e) {
+            const float r = rho[(size_t)key_idx(k) * IVF_RHO + shortlist - 1];
+            if (r < INFINITY) {
+                const float t = sqrtf(__uint_as_float(key_dist(k)) * (1.f + 1.f / 1024.f)) + r;
+                b = t * t;
+            }
+        }
+        sb[j] = b;
     }
     __syncthreads();
     if (!MLP) {
         if (j < np) probes[q * np + j] = sc[j];
+        if (qbound) write_probe_bound(j < np ? sb[j] : INFINITY, sqr, d, xmax, qbound, q, sred);
         return;
     }
     const __nv_bfloat16 *W1 = reinterpret_cast<const __nv_bfloat16 *>(w.W1);
@@ -983,6 +1040,7 @@ __global__ void __launch_bounds__(256) coarse_probe_kernel(const float *__restri
             if (lane == 0 && nprobed) nprobed[q] = total;
         }
     }
+    if (qbound) write_probe_bound(keep ? sb[i] : INFINITY, sqr, d, xmax, qbound, q, sred);
 }
 
 // Probes of the tensor-core engine: BF16 centroid scores on the tensor cores,
@@ -990,16 +1048,20 @@ __global__ void __launch_bounds__(256) coarse_probe_kernel(const float *__restri
 static int ivfl2_probes_tc(gn_index *ix, const float *dQ, int64_t nq, int *np_out, cudaStream_t st) {
     IvfL2State &S = *ix->ivfl2;
     IvfScratch &T = S.s;
+    // per query: the list scan's score bound (all ones: none, every score kept)
+    GN_TRY(T.qbound.ensure((size_t)std::max<int64_t>(nq, 1) * 4));
     if (S.nc < PROBER_CAND || S.d > PROBE_MAX_D || S.nc > 8192) {  // outside the 64-candidate stage's limits
         if (S.prober) return fail(GN_ERR_INVALID, "learned probing needs at least 64 lists");
         int np = std::min<int32_t>(S.nprobe, S.nc);
         *np_out = np;
+        GN_CUDA_TRY(cudaMemsetAsync(T.qbound.p, 0xff, (size_t)nq * 4, st));
         return ivfl2_coarse(ix, dQ, nq, np, st);
     }
     const bool mlp = S.prober != nullptr;
     const int np = mlp ? PROBER_CAND : std::min<int32_t>(std::min<int32_t>(S.nprobe, S.nc), PROBER_CAND);
     if (!mlp && S.nprobe > PROBER_CAND) {  // wider fixed probing: the FP32 coarse stage
         *np_out = std::min<int32_t>(S.nprobe, S.nc);
+        GN_CUDA_TRY(cudaMemsetAsync(T.qbound.p, 0xff, (size_t)nq * 4, st));
         return ivfl2_coarse(ix, dQ, nq, *np_out, st);
     }
     *np_out = np;
@@ -1038,11 +1100,15 @@ static int ivfl2_probes_tc(gn_index *ix, const float *dQ, int64_t nq, int *np_ou
         GN_TRY(T.nprobed.ensure((size_t)nq * 4));
         coarse_probe_kernel<true><<<(unsigned)nq, 256, ksm, st>>>(S.cscores.as<float>(), S.nc, ncp2, dQ, S.d, S.dp,
                                                                S.cent.as<float>(), nq, np, w, S.prober_tau,
-                                                               T.probes.as<int32_t>(), T.nprobed.as<int32_t>());
+                                                               T.probes.as<int32_t>(), T.nprobed.as<int32_t>(),
+                                                               S.rho.as<float>(), S.shortlist, S.xmax,
+                                                               T.qbound.as<uint32_t>());
     } else {
         coarse_probe_kernel<false><<<(unsigned)nq, 256, ksm, st>>>(S.cscores.as<float>(), S.nc, ncp2, dQ, S.d, S.dp,
                                                                 S.cent.as<float>(), nq, np, w, 0.f,
-                                                                T.probes.as<int32_t>(), nullptr);
+                                                                T.probes.as<int32_t>(), nullptr,
+                                                                S.rho.as<float>(), S.shortlist, S.xmax,
+                                                                T.qbound.as<uint32_t>());
     }
     GN_CUDA_TRY(cudaGetLastError());
     return GN_OK;
@@ -1074,8 +1140,65 @@ __global__ void x16_tiled_kernel(const float *__restrict__ X, int64_t n, int d, 
     out[((((p >> 7) * (K / 64) + kb) * 128 + (p & 127)) * 64 + e0) / 8] = *reinterpret_cast<const uint4 *>(v);
 }
 
+// Squared distance (FP32) of every list row to its list's centroid, warp per row.
+__global__ void row_centroid_dist_kernel(const float *__restrict__ X, int64_t n, int d, int dp,
+                                         const int64_t *__restrict__ list_off, int nc, const float *__restrict__ C,
+                                         float *__restrict__ out) {
+    const int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (r >= n) return;
+    int lo = 0, hi = nc;  // list l: list_off[l] <= r < list_off[l + 1]
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (list_off[mid] <= r) lo = mid;
+        else hi = mid;
+    }
+    float s = 0.f;
+    for (int t = lane; t < d; t += 32) {
+        const float e = X[r * dp + t] - C[(int64_t)lo * dp + t];
+        s = fmaf(e, e, s);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) out[r] = s;
+}
+
+// Inputs of the list scan's score bound (the probe stage turns them into a
+// per-query bound): per list, the distances to its centroid of the 64 rows
+// nearest it, ascending, each rounded up by a relative 2^-10 (covering the
+// FP32 sum's rounding); +inf past the list's size.  And the largest row norm.
+static int ivfl2_list_radii(IvfL2State &S, cudaStream_t st) {
+    std::vector<float> dist((size_t)S.n), nrm((size_t)S.n);
+    if (S.n > 0) {
+        DBuf tmp;
+        GN_TRY(tmp.ensure((size_t)S.n * 4));
+        row_centroid_dist_kernel<<<(unsigned)ceil_div(S.n * 32, 256), 256, 0, st>>>(
+            S.vecs.as<float>(), S.n, S.d, S.dp, S.list_off.as<int64_t>(), S.nc, S.cent.as<float>(), tmp.as<float>());
+        GN_CUDA_TRY(cudaGetLastError());
+        GN_CUDA_TRY(cudaMemcpyAsync(dist.data(), tmp.p, (size_t)S.n * 4, cudaMemcpyDeviceToHost, st));
+        GN_CUDA_TRY(cudaMemcpyAsync(nrm.data(), S.vnorm.p, (size_t)S.n * 4, cudaMemcpyDeviceToHost, st));
+        GN_CUDA_TRY(cudaStreamSynchronize(st));
+    }
+    std::vector<float> rho((size_t)S.nc * IVF_RHO, INFINITY);
+    for (int32_t l = 0; l < S.nc; ++l) {
+        float *b = dist.data() + S.h_off[(size_t)l], *e = dist.data() + S.h_off[(size_t)l + 1];
+        const int64_t m = std::min<int64_t>(IVF_RHO, e - b);
+        std::partial_sort(b, b + m, e);
+        for (int64_t j = 0; j < m; ++j)
+            rho[(size_t)l * IVF_RHO + j] = std::sqrt(std::max(0.f, b[j]) * (1.f + 1.f / 1024.f));
+    }
+    float x2 = 0.f;
+    for (float v : nrm) x2 = std::max(x2, v);
+    S.xmax = std::sqrt(x2 * (1.f + 1.f / 1024.f));
+    GN_TRY(S.rho.ensure(rho.size() * 4));
+    GN_CUDA_TRY(cudaMemcpyAsync(S.rho.p, rho.data(), rho.size() * 4, cudaMemcpyHostToDevice, st));
+    GN_CUDA_TRY(cudaStreamSynchronize(st));  // rho goes out of scope
+    return GN_OK;
+}
+
 int ivfl2_prepare_tc(gn_index *ix, cudaStream_t st) {
     IvfL2State &S = *ix->ivfl2;
+    GN_TRY(ivfl2_list_radii(S, st));
     S.K = (int)round_up(S.d, 64);
     // BF16 list rows, tiled (see IvfL2State::x16): padded list starts
     std::vector<int64_t> xo((size_t)S.nc + 1, 0);
@@ -1128,6 +1251,7 @@ int ivfl2_search_tc(gn_index *ix, const float *dQ, int64_t nq, int k, int64_t *d
     const int64_t qb_rows = std::max<int64_t>(npairs, 256);  // >= one 256-row TMA box
     GN_TRY(S.qb.ensure((size_t)qb_rows * S.K * 2));
     GN_TRY(S.aslot.ensure((size_t)npairs * 8));
+    GN_TRY(S.abound.ensure((size_t)std::max<int64_t>(npairs, 1) * 4));
     const int64_t maxlen = S.top_rows.size() > 1 ? S.top_rows[1] : 0;
     // sized for the shortest row chunk (256) so that a smaller batch never needs more
     const int64_t max_units = (ceil_div(npairs, qch) + S.nc) * (ceil_div(maxlen, 256) + 1);
@@ -1136,7 +1260,8 @@ int ivfl2_search_tc(gn_index *ix, const float *dQ, int64_t nq, int k, int64_t *d
     const unsigned qb_blocks = (unsigned)ceil_div(npairs, 8);
     qb_units_kernel<<<qb_blocks + (unsigned)ceil_div(max_units, 256), 256, 0, st>>>(
         S.q16.as<uint4>(), S.K / 8, np, T.bucket.as<int64_t>(), T.boff.as<int64_t>(), S.nc, T.qslot.as<int64_t>(),
-        T.slot_rel.as<int64_t>(), S.qb.as<uint4>(), S.aslot.as<int64_t>(), npairs, qb_blocks,
+        T.slot_rel.as<int64_t>(), S.qb.as<uint4>(), S.aslot.as<int64_t>(), T.qbound.as<uint32_t>(),
+        S.abound.as<uint32_t>(), npairs, qb_blocks,
         T.item_off.as<int64_t>(), S.list_off.as<int64_t>(), S.xoff.as<int64_t>(), rc, qch, max_units, S.units.as<TcUnit>(),
         S.nunits.as<int64_t>());
     // score slots: at most the rows of the np largest lists per query, plus one
@@ -1159,6 +1284,7 @@ int ivfl2_search_tc(gn_index *ix, const float *dQ, int64_t nq, int k, int64_t *d
     a.seg_mul = 128;
     a.scores = S.scores.as<float>();
     a.tmin4 = S.tmin.as<uint32_t>();
+    a.abound = S.abound.as<uint32_t>();
     a.err = S.err.as<int>();
     a.next_unit = S.sched.as<unsigned long long>() + 1;
     if (S.drill) {  // armed failure drill: this launch's waits run out after ~0.1 ms
@@ -1178,9 +1304,9 @@ int ivfl2_search_tc(gn_index *ix, const float *dQ, int64_t nq, int k, int64_t *d
     const int nsm = dev_info().num_sms;
     if (np <= 64 && tn.nt == 32) {
         ivf_tc_select_warp_kernel<<<(unsigned)ceil_div(nq, SELW_WARPS), 32 * SELW_WARPS, 0, st>>>(
-            S.scores.as<float>(), S.tmin.as<uint4>(), T.probes.as<int32_t>(), np, T.qslot.as<int64_t>(),
-            T.slot_rel.as<int64_t>(), S.list_off.as<int64_t>(), S.shortlist, dQ, S.vecs.as<float>(), S.d, S.dp,
-            S.ids.as<int32_t>(), nq, k, d_idx, d_dist, d_cnt);
+            S.scores.as<float>(), S.tmin.as<uint4>(), T.qbound.as<uint32_t>(), T.probes.as<int32_t>(), np,
+            T.qslot.as<int64_t>(), T.slot_rel.as<int64_t>(), S.list_off.as<int64_t>(), S.shortlist, dQ,
+            S.vecs.as<float>(), S.d, S.dp, S.ids.as<int32_t>(), nq, k, d_idx, d_dist, d_cnt);
         GN_CUDA_TRY(cudaGetLastError());
         return GN_OK;
     }
@@ -1207,8 +1333,8 @@ int ivfl2_search_tc(gn_index *ix, const float *dQ, int64_t nq, int k, int64_t *d
             carve = true;
         }
         ivf_tc_select_kernel<NT><<<blocks, NT, 0, st>>>(
-            S.scores.as<float>(), S.tmin.as<uint4>(), T.probes.as<int32_t>(), np, T.qslot.as<int64_t>(),
-            T.slot_rel.as<int64_t>(),
+            S.scores.as<float>(), S.tmin.as<uint4>(), T.qbound.as<uint32_t>(), T.probes.as<int32_t>(), np,
+            T.qslot.as<int64_t>(), T.slot_rel.as<int64_t>(),
             S.list_off.as<int64_t>(), S.shortlist, dQ, S.vecs.as<float>(), S.d, S.dp, S.ids.as<int32_t>(), nq, k, B,
             S.sel_part.as<uint64_t>(), S.sel_done.as<int>(), d_idx, d_dist, d_cnt);
         return GN_OK;

@@ -17,9 +17,13 @@
 //              within a set, thread = list row; for each query column its score
 //              |x|^2 - 2 q.x (exact FP32 |x|^2) goes to that (query, probe)
 //              pair's segment at the row's offset — 32 lanes write 32
-//              consecutive rows, so every store is one 128-byte line — and,
-//              for the list scan, the minimum score of each 32-row quarter
-//              of the 128-row tile goes to the pair's tile-minimum array.
+//              consecutive rows, so every store is one 128-byte line.  For
+//              the list scan, the minimum score of each 32-row quarter of the
+//              128-row tile goes to the pair's tile-minimum array, and the
+//              quarter's scores are stored only when that minimum is not
+//              above the query's score bound (an upper bound on its
+//              shortlist-th best score, from the probe stage): the other
+//              quarters hold no shortlist candidate and never reach memory.
 #include <cuda_bf16.h>
 
 #include <algorithm>
@@ -48,6 +52,18 @@ __device__ __forceinline__ uint32_t ti_ord(float f) {
     return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
 }
 
+// its inverse (ordered key -> float); keys above +inf's (all ones: no bound) give +inf
+__device__ __forceinline__ float ti_unord(uint32_t k) {
+    return k >= 0xff800000u ? INFINITY : __uint_as_float((k & 0x80000000u) ? (k & 0x7fffffffu) : ~k);
+}
+
+// minimum of v over the warp (every lane gets it)
+__device__ __forceinline__ float ti_warp_min(float v) {
+    float r;
+    asm("redux.sync.min.f32 %0, %1, 0xffffffff;" : "=f"(r) : "f"(v));
+    return r;
+}
+
 __device__ __forceinline__ int ti_nsel(int na) { return na <= 32 ? 32 : na <= 64 ? 64 : 128; }
 
 __global__ void __launch_bounds__(TI_THREADS, 1)
@@ -56,7 +72,8 @@ __global__ void __launch_bounds__(TI_THREADS, 1)
                   const TcUnit *__restrict__ units,
                   const int64_t *__restrict__ n_units_ptr, int K, const float *__restrict__ xnorm,
                   const int64_t *__restrict__ aslot, int seg_mul, float *__restrict__ scores,
-                  uint32_t *__restrict__ tmin4, int *__restrict__ err, unsigned long long *__restrict__ next_unit,
+                  uint32_t *__restrict__ tmin4, const uint32_t *__restrict__ abound, int *__restrict__ err,
+                  unsigned long long *__restrict__ next_unit,
                   long long wait_limit, int drill, int tiled) {
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
@@ -180,21 +197,34 @@ __global__ void __launch_bounds__(TI_THREADS, 1)
             const TcUnit un = units[u];
             const int nsel = ti_nsel(un.na);
             const int nchunk = nsel / 32;
-            // segment base (aslot x seg_mul, minus the list start) of query column c*32 + lane
+            // segment base (aslot x seg_mul, minus the list start) and score
+            // bound of query column c*32 + lane
             int64_t segv[TI_NMAX / 32 / 2];
+            float bndv[TI_NMAX / 32 / 2];
 #pragma unroll
             for (int cc = 0; cc < TI_NMAX / 32 / 2; ++cc) {
                 const int col = (grp + 2 * cc) * 32 + lane;
                 segv[cc] = (col < un.na) ? aslot[un.a0 + col] * seg_mul - un.rbase : INT64_MIN;
+                bndv[cc] = (col < un.na && abound) ? ti_unord(abound[un.a0 + col]) : INFINITY;
             }
             const int ntile = (int)((un.r1 - un.r0 + TI_M - 1) / TI_M);
+            // |x|^2 of this lane's row in tile t; rows past the list's end (zero
+            // rows of the tiled layout) score +inf.  Loaded one of the set's
+            // tiles ahead, so that a full accumulator never waits on it.
+            auto xload = [&](int t) -> float {
+                const int64_t rw = un.r0 + (int64_t)t * TI_M + quad * 32 + lane;
+                return rw < un.r1 ? __ldg(xnorm + rw) : INFINITY;
+            };
+            const int t_first = (set - (int)(tile_it & 1)) & 1;  // the set takes tiles t_first, t_first + 2, ...
+            float xn_next = t_first < ntile ? xload(t_first) : 0.f;
             for (int t = 0; t < ntile; ++t, ++tile_it) {
                 const int b = tile_it % TI_NACC;
                 if ((b & 1) != set) continue;  // the other set's tile
                 const uint32_t tph = (tile_it / TI_NACC) & 1;
                 const int64_t row = un.r0 + (int64_t)t * TI_M + quad * 32 + lane;
                 const bool rok = row < un.r1;
-                const float xn = rok ? __ldg(xnorm + row) : 0.f;
+                const float xn = xn_next;
+                if (t + 2 < ntile) xn_next = xload(t + 2);
                 if (!mbar_wait(accfull + b, tph, verr, wait_limit)) { ok = false; break; }
                 tc_fence_after();
 #pragma unroll 1
@@ -203,25 +233,44 @@ __global__ void __launch_bounds__(TI_THREADS, 1)
                     float acc[32];
                     tmem_ld32(tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(b * TI_NMAX + c * 32), acc);
                     int64_t sv = segv[0];
+                    float bv = bndv[0];
 #pragma unroll
                     for (int z = 1; z < TI_NMAX / 32 / 2; ++z)
-                        if (cc == z) sv = segv[z];
-                    uint32_t mymin = 0xffffffffu;  // lane j: this warp's 32-row minimum of column j
-#pragma unroll
-                    for (int j = 0; j < 32; ++j) {
-                        const int64_t seg = __shfl_sync(0xffffffffu, sv, j);
-                        const float v = fmaf(-2.f, acc[j], xn);
-                        if (seg != INT64_MIN && rok) scores[seg + row] = v;
-                        if (tmin4) {
-                            const uint32_t m = __reduce_min_sync(0xffffffffu, rok ? ti_ord(v) : 0xffffffffu);
-                            mymin = lane == j ? m : mymin;
+                        if (cc == z) {
+                            sv = segv[z];
+                            bv = bndv[z];
                         }
+#pragma unroll
+                    for (int j = 0; j < 32; ++j) acc[j] = fmaf(-2.f, acc[j], xn);  // the scores
+                    unsigned keep = 0xffffffffu;  // columns whose quarter is stored
+                    if (tmin4) {
+                        // the 32-row minimum of every column (one warp reduction each),
+                        // then lane j takes column j's by a select tree on its lane bits
+                        float m[32];
+#pragma unroll
+                        for (int j = 0; j < 32; ++j) m[j] = ti_warp_min(acc[j]);
+#pragma unroll
+                        for (int h = 16; h >= 1; h >>= 1)
+#pragma unroll
+                            for (int i = 0; i < h; ++i) m[i] = (lane & h) ? m[i + h] : m[i];
+                        const float mymin = m[0];
+                        // tile minimum, one word per 32-row quarter: slot = segment base / 128
+                        // + the tile's index in the list (segments are 128-aligned)
+                        if (sv != INT64_MIN) {
+                            const int64_t tile = (sv + un.rbase) / TI_M + (un.r0 - un.rbase) / TI_M + t;
+                            tmin4[tile * 4 + quad] = ti_ord(mymin);
+                        }
+                        // a quarter whose minimum is above its query's bound holds none
+                        // of the query's shortlist: its scores are not stored
+                        keep = __ballot_sync(0xffffffffu, sv != INT64_MIN && mymin <= bv);
                     }
-                    // tile minimum, one word per 32-row quarter: slot = segment base / 128
-                    // + the tile's index in the list (segments are 128-aligned)
-                    if (tmin4 && sv != INT64_MIN) {
-                        const int64_t tile = (sv + un.rbase) / TI_M + (un.r0 - un.rbase) / TI_M + t;
-                        tmin4[tile * 4 + quad] = mymin;
+                    if (keep) {
+#pragma unroll
+                        for (int j = 0; j < 32; ++j) {
+                            if (!((keep >> j) & 1u)) continue;  // warp-uniform
+                            const int64_t seg = __shfl_sync(0xffffffffu, sv, j);
+                            if (seg != INT64_MIN && rok) scores[seg + row] = acc[j];
+                        }
                     }
                 }
                 tc_fence_before();
@@ -264,7 +313,8 @@ int tc_ivf_launch(const TcIvfLaunch &a, cudaStream_t st) {
     if (!a.next_unit) return fail(GN_ERR_INVALID, "tensor-core list scan: no unit counter");
     GN_CUDA_TRY(cudaMemsetAsync(a.next_unit, 0, sizeof(unsigned long long), st));
     tc_ivf_kernel<<<a.grid, TI_THREADS, TI_SMEM, st>>>(mx, m32, m64, m128, a.units, a.n_units, a.K, a.xnorm,
-                                                        a.aslot, a.seg_mul, a.scores, a.tmin4, a.err, a.next_unit,
+                                                        a.aslot, a.seg_mul, a.scores, a.tmin4, a.abound, a.err,
+                                                        a.next_unit,
                                                         a.wait_limit > 0 ? a.wait_limit : TC_TIMEOUT_CYCLES, a.drill,
                                                         a.tiled);
     GN_CUDA_TRY(cudaGetLastError());

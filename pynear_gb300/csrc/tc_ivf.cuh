@@ -19,6 +19,9 @@ struct TcIvfLaunch {
     int seg_mul = 1;                // 128 for the list scan: segments are 128-row slots
     float *scores = nullptr;
     uint32_t *tmin4 = nullptr;      // optional: per (slot, 32-row quarter) minimum ordered score
+    // with tmin4: per query row, the ordered score bound of its query; a
+    // quarter's scores are stored only when its minimum is not above it
+    const uint32_t *abound = nullptr;
     int *err = nullptr;
     unsigned long long *next_unit = nullptr;  // device counter of the dynamic unit schedule (reset per launch)
     long long wait_limit = 0;       // cycles a pipeline wait may take (0: the default, about 2 s)
