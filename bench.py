@@ -57,7 +57,7 @@ CAL_TARGET = 0.955
 PROB_THRESHOLDS = [0.5, 0.4, 0.3, 0.25, 0.22, 0.2, 0.19, 0.18, 0.17, 0.16, 0.15, 0.12, 0.1, 0.05, 0.02]
 # concurrent search contexts: the index and LANES - 1 forks of it (shared lists,
 # own scratch), one stream each; a step's batches go to the lanes round-robin
-LANES = 4
+LANES = 8
 
 
 # ── environment helpers ───────────────────────────────────────────────────
@@ -1075,7 +1075,8 @@ def profile_case(name):
       ivf_mlp       the same index and batch with a learned prober attached
                     (untrained weights: the probe stage's fused MLP,
                     coarse_probe_kernel<1>, costs the same whatever they are);
-      tc_shortlist  1,000,000 x 128 mixture, 2,048 queries, BF16, shortlist 40;
+      tc_shortlist  1,000,000 x 128 mixture, 10,000 queries, BF16, shortlist 40
+                    (the benchmark's shortlist step, about 1 GB on the device);
       flat_l2_hbm   exact flat L2, 1,000,000 x 128 FP32, 8 queries;
       hamming       exact Hamming, 1,000,000 x 512 bits, 10,000 queries;
       voronoi       3840 x 2160 raster, 4,096 seeds.
@@ -1103,7 +1104,7 @@ def profile_case(name):
             _lib.check(lib.gn_ivfl2_search_knn_device(ix._h.h, vp(d_q), len(q), K, vp(o[0]), vp(o[1]), vp(o[2]),
                                                       ctypes.c_void_p(stream.cuda_stream)))
     elif name == "tc_shortlist":
-        db, q, _, _ = W.gaussian_mixture(n=1_000_000, d=128, n_centres=1024, sigma=0.3, zipf_s=0, nq=2048, seed=11)
+        db, q, _, _ = W.gaussian_mixture(n=1_000_000, d=128, n_centres=1024, sigma=0.3, zipf_s=0, nq=10_000, seed=11)
         ix = gn.FlatL2TCIndex(shortlist=40)
         ix.set(db)
         d_q = torch.from_numpy(q).to(dev)
@@ -1177,7 +1178,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gpunear", choices=["gpunear", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--lanes", type=int, default=4,
+    ap.add_argument("--lanes", type=int, default=LANES,
                     help="concurrent search contexts (the index and lanes - 1 forks, one stream each)")
     ap.add_argument("--profile-case", choices=PROFILE_CASES,
                     help="run one small case of one kernel inside a profiler region (for ncu) and exit")

@@ -7,9 +7,11 @@
 // list.  One persistent CTA per SM takes work units (list, chunk of <= 128
 // queries, chunk of rows) from an atomic counter, largest lists first; warp 0
 // hands each unit index to the other warps through a 4-slot ring of mbarriers:
-//   warp 0     TMA: per 64-wide K slice, 128 list rows (BF16) and the unit's
-//              N query rows (BF16, bucket order) into a 6-stage ring;
-//   warp 1     TMEM (4 accumulators x 128 columns) and tcgen05.mma M=128, N, K=16;
+//   warp 0     TMA: per 64-wide K slice, two tiles of 128 list rows (BF16)
+//              and the unit's N query rows (BF16, bucket order) into a
+//              4-stage ring — the queries are loaded once per tile pair;
+//   warp 1     TMEM (4 accumulators x 128 columns) and tcgen05.mma M=128, N,
+//              K=16, the pair's two tiles into two accumulators;
 //   warps 2-17 epilogue, two sets of eight: set e takes the tiles whose
 //              accumulator index is odd (e = 1) or even (e = 0), so two tiles
 //              are drained at once (the drain is latency-bound: more warps in
@@ -35,10 +37,12 @@
 
 namespace gn {
 
-constexpr int TI_M = 128, TI_NMAX = 128, TI_BK = 64, TI_STAGES = 6;
+constexpr int TI_M = 128, TI_NMAX = 128, TI_BK = 64, TI_STAGES = 4;
 constexpr int TI_A_BYTES = TI_M * TI_BK * 2;       // 16 KB
 constexpr int TI_B_BYTES = TI_NMAX * TI_BK * 2;    // 16 KB (max)
-constexpr int TI_STAGE_BYTES = TI_A_BYTES + TI_B_BYTES;
+// a stage holds one K slice of two row tiles (a tile pair) and of the unit's
+// queries: the queries' bytes are loaded once per two tiles
+constexpr int TI_STAGE_BYTES = 2 * TI_A_BYTES + TI_B_BYTES;
 constexpr int TI_NEPI = 16;   // epilogue warps: two sets of eight
 constexpr int TI_SET = 8;     // warps per set (4 TMEM lane quadrants x 2 column groups)
 constexpr int TI_NACC = 4;    // TMEM accumulators of TI_NMAX columns
@@ -126,9 +130,10 @@ __global__ void __launch_bounds__(TI_THREADS, 1)
                 const TcUnit un = units[u];
                 const int nsel = ti_nsel(un.na);
                 const CUtensorMap *mq = nsel == 32 ? &tmQ32 : nsel == 64 ? &tmQ64 : &tmQ128;
-                const uint32_t bytes = TI_A_BYTES + (uint32_t)nsel * TI_BK * 2;
                 const int ntile = (int)((un.r1 - un.r0 + TI_M - 1) / TI_M);
-                for (int t = 0; t < ntile && ok; ++t) {
+                for (int t = 0; t < ntile && ok; t += 2) {  // tile pairs (the last may be single)
+                    const int nt = t + 1 < ntile ? 2 : 1;
+                    const uint32_t bytes = (uint32_t)nt * TI_A_BYTES + (uint32_t)nsel * TI_BK * 2;
                     for (int kb = 0; kb < nk; ++kb, ++it) {
                         const int s = it % TI_STAGES;
                         const uint32_t ph = (it / TI_STAGES) & 1;
@@ -136,11 +141,15 @@ __global__ void __launch_bounds__(TI_THREADS, 1)
                         uint8_t *sa = smem + s * TI_STAGE_BYTES;
                         if (drill) continue;  // failure drill: no copies, so the MMA's waits run out
                         mbar_expect_tx(full + s, bytes);
-                        if (tiled)  // the tile's K slice kb: one contiguous 16 KB block
-                            tma_load_2d(sa, &tmX, 0, (int)((((un.xrow >> 7) + t) * nk + kb) * TI_M), full + s);
-                        else
-                            tma_load_2d(sa, &tmX, kb * TI_BK, (int)(un.r0 + (int64_t)t * TI_M), full + s);
-                        tma_load_2d(sa + TI_A_BYTES, mq, kb * TI_BK, (int)un.a0, full + s);
+                        for (int h = 0; h < nt; ++h) {
+                            if (tiled)  // the tile's K slice kb: one contiguous 16 KB block
+                                tma_load_2d(sa + h * TI_A_BYTES, &tmX, 0,
+                                            (int)((((un.xrow >> 7) + t + h) * nk + kb) * TI_M), full + s);
+                            else
+                                tma_load_2d(sa + h * TI_A_BYTES, &tmX, kb * TI_BK,
+                                            (int)(un.r0 + (int64_t)(t + h) * TI_M), full + s);
+                        }
+                        tma_load_2d(sa + 2 * TI_A_BYTES, mq, kb * TI_BK, (int)un.a0, full + s);
                     }
                 }
             }
@@ -159,25 +168,36 @@ __global__ void __launch_bounds__(TI_THREADS, 1)
                 const int nsel = ti_nsel(un.na);
                 const uint32_t idesc = idesc_bf16_f32(TI_M, nsel);
                 const int ntile = (int)((un.r1 - un.r0 + TI_M - 1) / TI_M);
-                for (int t = 0; t < ntile && ok; ++t, ++tile_it) {
-                    const int b = tile_it % TI_NACC;
-                    const uint32_t tph = (tile_it / TI_NACC) & 1;
-                    if (!mbar_wait(accempty + b, tph ^ 1, verr, wait_limit)) { ok = false; break; }
+                for (int t = 0; t < ntile && ok; t += 2) {  // tile pairs: two accumulators, one B
+                    const int nt = t + 1 < ntile ? 2 : 1;
+                    uint32_t dt[2];
+                    int bb[2];
+                    for (int h = 0; h < nt && ok; ++h) {
+                        bb[h] = (tile_it + h) % TI_NACC;
+                        const uint32_t tph = ((tile_it + h) / TI_NACC) & 1;
+                        if (!mbar_wait(accempty + bb[h], tph ^ 1, verr, wait_limit)) ok = false;
+                        dt[h] = tmem + (uint32_t)(bb[h] * TI_NMAX);
+                    }
+                    if (!ok) break;
                     tc_fence_after();
-                    const uint32_t dt = tmem + (uint32_t)(b * TI_NMAX);
                     for (int kb = 0; kb < nk; ++kb, ++it) {
                         const int s = it % TI_STAGES;
                         const uint32_t ph = (it / TI_STAGES) & 1;
                         if (!mbar_wait(full + s, ph, verr, wait_limit)) { ok = false; break; }
                         tc_fence_after();
                         const uint32_t sa = smem_u32(smem + s * TI_STAGE_BYTES);
-                        const uint64_t da = sdesc_sw128(sa), db = sdesc_sw128(sa + TI_A_BYTES);
+                        const uint64_t db = sdesc_sw128(sa + 2 * TI_A_BYTES);
+                        for (int h = 0; h < nt; ++h) {
+                            const uint64_t da = sdesc_sw128(sa + h * TI_A_BYTES);
 #pragma unroll
-                        for (int kk = 0; kk < TI_BK / 16; ++kk)
-                            umma_bf16(dt, da + 2 * kk, db + 2 * kk, idesc, (kb | kk) ? 1u : 0u);
+                            for (int kk = 0; kk < TI_BK / 16; ++kk)
+                                umma_bf16(dt[h], da + 2 * kk, db + 2 * kk, idesc, (kb | kk) ? 1u : 0u);
+                        }
                         umma_commit(empty + s);
                     }
-                    if (ok) umma_commit(accfull + b);
+                    if (!ok) break;
+                    for (int h = 0; h < nt; ++h) umma_commit(accfull + bb[h]);
+                    tile_it += nt;
                 }
             }
         }

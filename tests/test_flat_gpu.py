@@ -220,3 +220,35 @@ def test_pickle_roundtrip(gn):
     a = ix.searchKNN(q, 4)
     ix2 = pickle.loads(pickle.dumps(ix))
     assert ix2.searchKNN(q, 4) == a
+
+
+@pytest.mark.parametrize("nq", [1, 3, 4, 5, 8])
+def test_small_batches(gn, oracle, nq):
+    """Batches of at most 8 queries (the scan's one- and two-query-per-warp
+    layouts): every width up to 129, odd ones included, and k up to 32."""
+    rng = np.random.default_rng(100 + nq)
+    for d in (1, 5, 17, 32, 63, 64, 100, 128, 129):
+        db = (rng.random((3000, d), dtype=np.float32) * 4 - 2)
+        q = (rng.random((nq, d), dtype=np.float32) * 4 - 2)
+        for metric in ("l2", "l1", "linf"):
+            ix = _flat(gn, metric, db)
+            for k in (1, 7, 32):
+                idx, dist = ix.search_knn_arrays(q, k)
+                oi, od = oracle.knn_float(metric, db, q, k)
+                assert np.array_equal(idx, oi), (metric, d, k)
+                assert np.array_equal(_bits(dist), _bits(od)), (metric, d, k)
+
+
+def test_exact_l2_1m_x128_8_queries(gn, oracle):
+    """The HBM-bound case of the benchmark: 1,000,000 x 128 N(0,1) rows, 8
+    queries, k 10 (about 2,000 row slices merged per query), bit-exact
+    against the oracle."""
+    rng = np.random.default_rng(17)
+    db = rng.standard_normal((1_000_000, 128), dtype=np.float32)
+    q = rng.standard_normal((8, 128), dtype=np.float32)
+    ix = gn.FlatL2Index()
+    ix.set(db)
+    idx, dist = ix.search_knn_arrays(q, 10)
+    oi, od = oracle.knn_float("l2", db, q, 10)
+    assert np.array_equal(idx, oi)
+    assert np.array_equal(_bits(dist), _bits(od))
