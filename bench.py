@@ -1060,7 +1060,7 @@ def run_reference(args):
 
 
 # ── small profiling cases (one profiler region around exactly one call) ─────
-PROFILE_CASES = ("ivf_scan", "ivf_mlp", "tc_shortlist", "flat_l2_hbm", "hamming", "voronoi")
+PROFILE_CASES = ("ivf_scan", "ivf_mlp", "ivf_1m", "tc_shortlist", "flat_l2", "flat_l2_hbm", "hamming", "voronoi")
 
 
 def profile_case(name):
@@ -1075,8 +1075,16 @@ def profile_case(name):
       ivf_mlp       the same index and batch with a learned prober attached
                     (untrained weights: the probe stage's fused MLP,
                     coarse_probe_kernel<1>, costs the same whatever they are);
+      ivf_1m        the benchmark's index (1,000,000 x 512, 2,048 centres, nlist
+                    1,024) and tuned configuration: the prober trained as the
+                    benchmark trains it (200,000 labelled mixture queries, 4
+                    epochs) at probability threshold 0.19 (the benchmark
+                    calibrates to about 0.191), one 4,096-query batch; several
+                    GB on the device, so only one-pass metrics (the list scan's
+                    DRAM bytes) are captured on it;
       tc_shortlist  1,000,000 x 128 mixture, 10,000 queries, BF16, shortlist 40
                     (the benchmark's shortlist step, about 1 GB on the device);
+      flat_l2       exact flat L2, 100,000 x 32 uniform, 1,000 queries, k 5;
       flat_l2_hbm   exact flat L2, 1,000,000 x 128 FP32, 8 queries;
       hamming       exact Hamming, 1,000,000 x 512 bits, 10,000 queries;
       voronoi       3840 x 2160 raster, 4,096 seeds.
@@ -1089,12 +1097,27 @@ def profile_case(name):
     dev = torch.device("cuda", 0)
     stream = torch.cuda.current_stream(dev)
     info = {"case": name}
-    if name in ("ivf_scan", "ivf_mlp"):
-        db, q, _, _ = W.gaussian_mixture(n=400_000, d=512, n_centres=820, sigma=0.3, zipf_s=1.1, nq=4096, seed=3)
-        ix = gn.IVFFlatL2Index(n_clusters=410, n_probe=11, engine="tc")
+    if name in ("ivf_scan", "ivf_mlp", "ivf_1m"):
+        if name == "ivf_1m":
+            db, q, _, _ = W.gaussian_mixture(n=IVF_N, d=IVF_D, n_centres=IVF_CENTRES, sigma=0.3, zipf_s=1.1,
+                                             nq=4096, seed=0)
+            ix = gn.IVFFlatL2Index(n_clusters=IVF_NLIST, n_probe=11, engine="tc")
+        else:
+            db, q, _, _ = W.gaussian_mixture(n=400_000, d=512, n_centres=820, sigma=0.3, zipf_s=1.1, nq=4096, seed=3)
+            ix = gn.IVFFlatL2Index(n_clusters=410, n_probe=11, engine="tc")
         ix.set(db)
         if name == "ivf_mlp":
             ix.set_prober(gn.LearnedProber(ix, seed=1), 0.5)
+        if name == "ivf_1m":
+            train_q = W.gaussian_mixture_queries(n=IVF_N, d=IVF_D, n_centres=IVF_CENTRES, sigma=0.3, zipf_s=1.1,
+                                                 nq=N_TRAIN, seed=0, query_seed=99991)
+            tcx = gn.FlatL2TCIndex(shortlist=40)
+            tcx.set(db)
+            gt = np.concatenate([tcx.search_knn_arrays(train_q[i:i + 20000], K)[0] for i in range(0, N_TRAIN, 20000)])
+            del tcx
+            pr = gn.LearnedProber(ix, seed=1)
+            pr.train(train_q, gt, epochs=4, batch=1024, lr=2e-3)
+            ix.set_prober(pr, 0.19)
         d_q = torch.from_numpy(q).to(dev)
         o = (torch.empty((len(q), K), dtype=torch.int64, device=dev),
              torch.empty((len(q), K), dtype=torch.float32, device=dev),
@@ -1114,6 +1137,17 @@ def profile_case(name):
         def call():
             _lib.check(lib.gn_tcflat_search_knn_device(ix._h.h, vp(d_q), len(q), K, vp(o[0]), vp(o[1]),
                                                        ctypes.c_void_p(stream.cuda_stream)))
+    elif name == "flat_l2":
+        db, q = W.uniform_l2(n=100_000, d=32, nq=1000, seed=7)
+        ix = gn.FlatL2Index()
+        ix.set(db)
+        d_q = torch.from_numpy(q).to(dev)
+        o = (torch.empty((len(q), 5), dtype=torch.int64, device=dev),
+             torch.empty((len(q), 5), dtype=torch.float32, device=dev))
+
+        def call():
+            _lib.check(lib.gn_flat_search_knn_device(ix._h.h, vp(d_q), len(q), 5, vp(o[0]), vp(o[1]),
+                                                     ctypes.c_void_p(stream.cuda_stream)))
     elif name == "flat_l2_hbm":
         rng = np.random.default_rng(17)
         db = rng.standard_normal((1_000_000, 128), dtype=np.float32)
@@ -1162,7 +1196,7 @@ def profile_case(name):
     call()
     torch.cuda.synchronize()
     torch.cuda.profiler.stop()
-    if name in ("ivf_scan", "ivf_mlp"):
+    if name in ("ivf_scan", "ivf_mlp", "ivf_1m"):
         w = np.zeros(4, np.int64)
         _lib.check(lib.gn_ivfl2_last_work(ix._h.h, w.ctypes.data_as(ctypes.c_void_p)))
         info.update(pairs=int(w[0]), scored_rows=int(w[1]), distinct_list_rows=int(w[2]), units=int(w[3]),

@@ -127,18 +127,22 @@ inline size_t fs_smem_bytes(int warps, int qw, int dp4) {
     return (size_t)warps * qw * dp4 * 16 + 1024 + FS_STAGES * fs_stage_bytes(dp4) + FS_STAGES * 8;
 }
 
-template <int METRIC, int QW, int R>
-__global__ void __launch_bounds__(128) float_scan_kernel(const __grid_constant__ CUtensorMap tm, int64_t n, int d,
-                                                         int dp, const float *__restrict__ q, int64_t nq, int k,
-                                                         int n_slices, int64_t slice_rows, int n_groups,
+// DW: the row width when known at compile time (32, 64 or 128 floats, no
+// padding): every shared-memory address and loop bound becomes a constant, so
+// the inner loop is the arithmetic and the loads alone; 0 = any width.
+template <int METRIC, int QW, int R, int DW = 0>
+__global__ void __launch_bounds__(128) float_scan_kernel(const __grid_constant__ CUtensorMap tm, int64_t n,
+                                                         int d_arg, int dp, const float *__restrict__ q, int64_t nq,
+                                                         int k, int n_slices, int64_t slice_rows, int n_groups,
                                                          uint64_t *__restrict__ part, int *__restrict__ err) {
+    const int d = DW ? DW : d_arg;
     extern __shared__ float4 sqf[];  // [WARPS*QW][dp/4] queries, then the stage ring
     const int warps = blockDim.x >> 5;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int unit = blockIdx.x;
     const int slice = unit / n_groups, group = unit % n_groups;
     const int64_t q0 = (int64_t)group * warps * QW;
-    const int dp4 = dp >> 2;
+    const int dp4 = DW ? DW / 4 : dp >> 2;
     const FsGeom g = fs_geom(dp4);
     const uint32_t box_bytes = (uint32_t)g.rows * g.bw * 4;
     const uint32_t stage_bytes = (uint32_t)g.cb * box_bytes;
@@ -410,12 +414,20 @@ static int launch_scan(const FlatScanArgs &a, int n_groups, int threads, size_t 
                               (uint64_t)a.stride4 * 16, (uint32_t)fg.bw, (uint32_t)fg.rows,
                               fg.bw == FS_BOX ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_NONE));
         timing_begin(st, "float_scan_kernel");
+        // rows of exactly 32, 64 or 128 floats with k <= 32: the width as a compile-time constant
+        const int dw = (R == 1 && a.d == a.stride4 * 4 && (a.d == 32 || a.d == 64 || a.d == 128)) ? a.d : 0;
         auto go = [&](auto MC, auto QC) {
             constexpr int Mv = decltype(MC)::value, Qv = decltype(QC)::value;
-            auto kern = float_scan_kernel<Mv, Qv, (Qv == 4 ? R : 1)>;
-            if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-            kern<<<units, threads, smem, st>>>(tm, a.n, a.d, a.stride4 * 4, reinterpret_cast<const float *>(a.q),
-                                               a.nq, a.k, a.n_slices, a.slice_rows, n_groups, part, a.err);
+            auto launch = [&](auto kern) {
+                if (smem > 48 * 1024)
+                    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+                kern<<<units, threads, smem, st>>>(tm, a.n, a.d, a.stride4 * 4, reinterpret_cast<const float *>(a.q),
+                                                   a.nq, a.k, a.n_slices, a.slice_rows, n_groups, part, a.err);
+            };
+            if (R == 1 && dw == 32) launch(float_scan_kernel<Mv, Qv, 1, 32>);
+            else if (R == 1 && dw == 64) launch(float_scan_kernel<Mv, Qv, 1, 64>);
+            else if (R == 1 && dw == 128) launch(float_scan_kernel<Mv, Qv, 1, 128>);
+            else launch(float_scan_kernel<Mv, Qv, (Qv == 4 ? R : 1)>);
         };
         auto by_qw = [&](auto MC) {
             // fewer queries per warp only for small batches with k <= 32 (R == 1)

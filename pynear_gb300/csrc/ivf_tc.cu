@@ -178,6 +178,7 @@ __device__ __forceinline__ void l2sq_warp_rows(const float *__restrict__ q, cons
 
 constexpr int SEL_PCH = 256;   // probes staged per pass
 constexpr int SEL_WB = 512;    // candidate keys buffered per warp
+constexpr int SEL_QCAP = 256;  // qualifying quarters listed from the threshold's staged minima
 
 // Ascending bitonic sort of n (power of two, <= 512) keys in shared memory by
 // one warp.
@@ -321,6 +322,33 @@ __device__ uint32_t block_kth_u32(const uint32_t *v, int n, int kth, int *hist, 
     return prefix;
 }
 
+// Offer each lane's key (want: it is a real row) to the warp's shared-memory
+// buffer W of SEL_WB keys (wn keys held, warp-uniform): keys below the warp
+// threshold are appended; a full buffer is sorted and cut to its best S, its
+// S-th key becoming the new threshold, and the keys that did not fit are
+// offered again.
+__device__ __forceinline__ void sel_buffer_offer(uint64_t key, bool want, uint64_t *W, int &wn, uint64_t &wthr,
+                                                 int S, int lane) {
+    bool w = want && key < wthr;
+    while (true) {
+        const unsigned b2 = __ballot_sync(0xffffffffu, w);
+        if (!b2) break;
+        const int pos = wn + __popc(b2 & ((1u << lane) - 1u));
+        if (w && pos < SEL_WB) {
+            W[pos] = key;
+            w = false;
+        }
+        wn += __popc(b2);
+        if (wn <= SEL_WB) break;
+        __syncwarp();
+        warp_bitonic_sort(W, SEL_WB, lane);
+        wthr = W[S - 1];
+        wn = S;
+        w = w && key < wthr;
+        __syncwarp();
+    }
+}
+
 // Selection of one query by B blocks of NT threads (B = 1 for large batches;
 // small batches split each query's range over up to 16 blocks, whose partial
 // best-S lists the last block to finish merges).  The list scan leaves, per
@@ -355,7 +383,8 @@ __global__ void __launch_bounds__(NT, 1024 / NT) ivf_tc_select_kernel(
     __shared__ int64_t w_sum[NW];
     __shared__ uint64_t sel[64], s_rk[64];
     __shared__ int hist[256], sh[4], s_wn[NW];
-    __shared__ int s_last;
+    __shared__ int s_last, s_qn;
+    __shared__ int32_t qlist[SEL_QCAP];
     const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
     const int64_t q = blockIdx.x / B;
     const int bq = (int)(blockIdx.x % B);  // this block's share of the query's slots (B > 1 needs np <= SEL_PCH)
@@ -365,6 +394,7 @@ __global__ void __launch_bounds__(NT, 1024 / NT) ivf_tc_select_kernel(
     uint32_t tau = 0xffffffffu;
 
     for (int p0 = 0; p0 < np; p0 += SEL_PCH) {
+        int64_t sweep_lo;  // first slot of this pass the sweep reads minima for
         const int pc = min(SEL_PCH, np - p0);
         // per-probe metadata and the prefix sum of the slot counts
         int64_t nslot = 0;
@@ -399,6 +429,7 @@ __global__ void __launch_bounds__(NT, 1024 / NT) ivf_tc_select_kernel(
         // threshold comes from enough slot minima (idle parts publish nothing)
         const int bu = (int)max((int64_t)1, min((int64_t)B, all / (2 * S)));
         const int64_t lo = bq < bu ? all * bq / bu : all, hi = bq < bu ? all * (bq + 1) / bu : all;
+        sweep_lo = lo;
         if (p0 == 0) {
             // threshold from the quarter minima of the block's first slots (any
             // S of them are S distinct rows' scores, so they bound it)
@@ -418,10 +449,52 @@ __global__ void __launch_bounds__(NT, 1024 / NT) ivf_tc_select_kernel(
             // and never above the query's bound: quarters above it were not stored
             tau = min(block_kth_u32<NT>(tm, 4 * ns, S, hist, sh), qbound[q]);
             wthr = tau == 0xffffffffu ? KEY_EMPTY : make_key(tau, 0xffffffffu);
+            // the qualifying quarters among the staged minima, listed (any order)
+            if (t == 0) s_qn = 0;
+            __syncthreads();
+            for (int i = t; i < 4 * ns; i += NT)
+                if (tm[i] <= tau) {
+                    const int pos = atomicAdd(&s_qn, 1);
+                    if (pos < SEL_QCAP) qlist[pos] = i;
+                }
+            __syncthreads();
+            // all of them listed: they are read straight from the list, four
+            // quarters per warp at a time with their loads in flight together;
+            // the sweep below covers the slots past the staged ones
+            if (s_qn <= SEL_QCAP) {
+                const int nl = s_qn;
+                for (int e0 = warp * 4; e0 < nl; e0 += NW * 4) {
+                    const int nb = min(4, nl - e0);
+                    uint64_t key[4];
+                    bool want[4];
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) {
+                        const int idx = u < nb ? qlist[e0 + u] : 0;
+                        const int64_t f = lo + (idx >> 2);
+                        int a = 0, b = pc;  // probe pp: p_tpre[pp] <= f < p_tpre[pp + 1]
+                        while (b - a > 1) {
+                            const int mid = (a + b) >> 1;
+                            if (p_tpre[mid] <= f) a = mid;
+                            else b = mid;
+                        }
+                        const int64_t slot = f - p_tpre[a];
+                        const int i = (idx & 3) * 32 + lane;  // row within the slot
+                        const int64_t r0 = slot * 128;
+                        const bool ok = u < nb && r0 + i < p_len[a];
+                        const uint32_t v = ok ? f2ord(__ldg(scores + (p_slot[a] + slot) * 128 + i)) : 0xffffffffu;
+                        key[u] = make_key(v, (uint32_t)(p_lb[a] + r0 + i));
+                        want[u] = ok;
+                    }
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) sel_buffer_offer(key[u], want[u], W, wn, wthr, S, lane);
+                }
+                sweep_lo = lo + ns;
+            }
+            __syncthreads();  // the list and the staged minima are done with before the buffers fill
         }
         int p = 0;  // probe of this lane's slot (monotone over the sweep)
         // warp w takes 8 slots at a time: lane l looks at quarter l % 4 of slot g0 + l / 4
-        for (int64_t g0 = lo + (int64_t)warp * 8; g0 < hi; g0 += (int64_t)NW * 8) {
+        for (int64_t g0 = sweep_lo + (int64_t)warp * 8; g0 < hi; g0 += (int64_t)NW * 8) {
             const int64_t f = g0 + (lane >> 2);
             const int qu = lane & 3;
             bool qual = false;
@@ -457,27 +530,7 @@ __global__ void __launch_bounds__(NT, 1024 / NT) ivf_tc_select_kernel(
                     want[u] = ok;
                 }
 #pragma unroll
-                for (int u = 0; u < 4; ++u) {
-                    bool w = want[u] && key[u] < wthr;
-                    while (true) {
-                        const unsigned b2 = __ballot_sync(0xffffffffu, w);
-                        if (!b2) break;
-                        const int pos = wn + __popc(b2 & ((1u << lane) - 1u));
-                        if (w && pos < SEL_WB) {
-                            W[pos] = key[u];
-                            w = false;
-                        }
-                        wn += __popc(b2);
-                        if (wn <= SEL_WB) break;
-                        // full: keep the best S; keys that did not fit are offered again
-                        __syncwarp();
-                        warp_bitonic_sort(W, SEL_WB, lane);
-                        wthr = W[S - 1];
-                        wn = S;
-                        w = w && key[u] < wthr;
-                        __syncwarp();
-                    }
-                }
+                for (int u = 0; u < 4; ++u) sel_buffer_offer(key[u], want[u], W, wn, wthr, S, lane);
             }
         }
         __syncthreads();
