@@ -1060,7 +1060,8 @@ def run_reference(args):
 
 
 # ── small profiling cases (one profiler region around exactly one call) ─────
-PROFILE_CASES = ("ivf_scan", "ivf_mlp", "ivf_1m", "tc_shortlist", "flat_l2", "flat_l2_hbm", "hamming", "voronoi")
+PROFILE_CASES = ("ivf_scan", "ivf_mlp", "ivf_1m", "ivf_step", "tc_shortlist", "flat_l2", "flat_l2_hbm", "hamming",
+                 "voronoi")
 
 
 def profile_case(name):
@@ -1082,6 +1083,10 @@ def profile_case(name):
                     calibrates to about 0.191), one 4,096-query batch; several
                     GB on the device, so only one-pass metrics (the list scan's
                     DRAM bytes) are captured on it;
+      ivf_step      the same index and prober (built-in launch choices, not
+                    autotuned, so that the launch list does not depend on the
+                    tuner's timing noise) and one step of the benchmark's 30
+                    log-uniform batches (16,384 queries) on one stream;
       tc_shortlist  1,000,000 x 128 mixture, 10,000 queries, BF16, shortlist 40
                     (the benchmark's shortlist step, about 1 GB on the device);
       flat_l2       exact flat L2, 100,000 x 32 uniform, 1,000 queries, k 5;
@@ -1097,10 +1102,10 @@ def profile_case(name):
     dev = torch.device("cuda", 0)
     stream = torch.cuda.current_stream(dev)
     info = {"case": name}
-    if name in ("ivf_scan", "ivf_mlp", "ivf_1m"):
-        if name == "ivf_1m":
+    if name in ("ivf_scan", "ivf_mlp", "ivf_1m", "ivf_step"):
+        if name in ("ivf_1m", "ivf_step"):
             db, q, _, _ = W.gaussian_mixture(n=IVF_N, d=IVF_D, n_centres=IVF_CENTRES, sigma=0.3, zipf_s=1.1,
-                                             nq=4096, seed=0)
+                                             nq=STEP_QUERIES if name == "ivf_step" else 4096, seed=0)
             ix = gn.IVFFlatL2Index(n_clusters=IVF_NLIST, n_probe=11, engine="tc")
         else:
             db, q, _, _ = W.gaussian_mixture(n=400_000, d=512, n_centres=820, sigma=0.3, zipf_s=1.1, nq=4096, seed=3)
@@ -1108,7 +1113,7 @@ def profile_case(name):
         ix.set(db)
         if name == "ivf_mlp":
             ix.set_prober(gn.LearnedProber(ix, seed=1), 0.5)
-        if name == "ivf_1m":
+        if name in ("ivf_1m", "ivf_step"):
             train_q = W.gaussian_mixture_queries(n=IVF_N, d=IVF_D, n_centres=IVF_CENTRES, sigma=0.3, zipf_s=1.1,
                                                  nq=N_TRAIN, seed=0, query_seed=99991)
             tcx = gn.FlatL2TCIndex(shortlist=40)
@@ -1118,14 +1123,19 @@ def profile_case(name):
             pr = gn.LearnedProber(ix, seed=1)
             pr.train(train_q, gt, epochs=4, batch=1024, lr=2e-3)
             ix.set_prober(pr, 0.19)
+
         d_q = torch.from_numpy(q).to(dev)
         o = (torch.empty((len(q), K), dtype=torch.int64, device=dev),
              torch.empty((len(q), K), dtype=torch.float32, device=dev),
              torch.empty((len(q),), dtype=torch.int64, device=dev))
+        batches = W.log_uniform_batches(STEP_QUERIES, 1, 4096, seed=1) if name == "ivf_step" else [len(q)]
+        offs = np.concatenate([[0], np.cumsum(batches)])
 
         def call():
-            _lib.check(lib.gn_ivfl2_search_knn_device(ix._h.h, vp(d_q), len(q), K, vp(o[0]), vp(o[1]), vp(o[2]),
-                                                      ctypes.c_void_p(stream.cuda_stream)))
+            for b0, nb in zip(offs[:-1], batches):
+                qp = ctypes.c_void_p(d_q.data_ptr() + int(b0) * q.shape[1] * 4)
+                _lib.check(lib.gn_ivfl2_search_knn_device(ix._h.h, qp, int(nb), K, vp(o[0]), vp(o[1]), vp(o[2]),
+                                                          ctypes.c_void_p(stream.cuda_stream)))
     elif name == "tc_shortlist":
         db, q, _, _ = W.gaussian_mixture(n=1_000_000, d=128, n_centres=1024, sigma=0.3, zipf_s=0, nq=10_000, seed=11)
         ix = gn.FlatL2TCIndex(shortlist=40)
@@ -1196,7 +1206,7 @@ def profile_case(name):
     call()
     torch.cuda.synchronize()
     torch.cuda.profiler.stop()
-    if name in ("ivf_scan", "ivf_mlp", "ivf_1m"):
+    if name in ("ivf_scan", "ivf_mlp", "ivf_1m"):  # the call's one batch
         w = np.zeros(4, np.int64)
         _lib.check(lib.gn_ivfl2_last_work(ix._h.h, w.ctypes.data_as(ctypes.c_void_p)))
         info.update(pairs=int(w[0]), scored_rows=int(w[1]), distinct_list_rows=int(w[2]), units=int(w[3]),

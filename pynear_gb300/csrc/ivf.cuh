@@ -12,7 +12,8 @@ constexpr int IVF_RHO = 64;  // per list: radii of its rows nearest the centroid
 // Per-batch scratch of an IVF search (device resident, reused).
 struct IvfScratch {
     DBuf q, qn, probes, probes64, pdist, bcnt, boff, bucket, fill, slot_rel, qcount, qslot, item_off, counter, part,
-        cpart, nprobed, qbound;  // qbound: per query, the ordered score bound of the tensor-core list scan
+        cpart, nprobed, qbound,  // qbound: per query, the ordered score bound of the tensor-core list scan
+        mh1, mcand, mcb, mqn;    // batched prober MLP: first-layer outputs, candidates, their bounds, |q|^2
 };
 
 // Float IVF (forest.py IVFFlatL2Index semantics, squared L2).

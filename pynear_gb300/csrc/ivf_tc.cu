@@ -844,6 +844,13 @@ constexpr int PROBE_MAX_D = 2048;  // query row staged in shared memory
 // 0.03 |q| xmax + 2^-12 (xmax + |q|)^2 and rounds every other term outwards.
 // Block-wide (all threads call it); thread 0 writes the ordered bound, or all
 // ones when there is none.
+__device__ __forceinline__ uint32_t probe_bound_key(float D, float qn, float xmax) {
+    const float qa = sqrtf(qn);
+    const float B = D * (1.f + 1.f / 1024.f) - qn * (1.f - 1.f / 1024.f) + 0.03f * qa * xmax +
+                    (xmax + qa) * (xmax + qa) * (1.f / 4096.f);
+    return (B < INFINITY && B == B) ? f2ord(B) : 0xffffffffu;
+}
+
 __device__ __forceinline__ void write_probe_bound(float b, const float *sqr, int d, float xmax,
                                                   uint32_t *__restrict__ qbound, int64_t q, float *red) {
     const int j = threadIdx.x, lane = j & 31, warp = j >> 5;
@@ -858,12 +865,7 @@ __device__ __forceinline__ void write_probe_bound(float b, const float *sqr, int
     }
     if (lane == 0 && warp < 2) red[warp] = b;
     __syncthreads();
-    if (j == 0) {
-        const float D = fminf(red[0], red[1]), qn = red[2], qa = sqrtf(qn);
-        const float B = D * (1.f + 1.f / 1024.f) - qn * (1.f - 1.f / 1024.f) + 0.03f * qa * xmax +
-                        (xmax + qa) * (xmax + qa) * (1.f / 4096.f);
-        qbound[q] = (B < INFINITY && B == B) ? f2ord(B) : 0xffffffffu;
-    }
+    if (j == 0) qbound[q] = probe_bound_key(fminf(red[0], red[1]), red[2], xmax);
 }
 
 // Per query (block of 256 threads): the 64 best centroids by BF16 score, their
@@ -877,7 +879,9 @@ __global__ void __launch_bounds__(256) coarse_probe_kernel(const float *__restri
                                                            int32_t *__restrict__ probes,
                                                            int32_t *__restrict__ nprobed,
                                                            const float *__restrict__ rho, int shortlist, float xmax,
-                                                           uint32_t *__restrict__ qbound) {
+                                                           uint32_t *__restrict__ qbound, float *__restrict__ h1_out,
+                                                           int32_t *__restrict__ cand_out,
+                                                           float *__restrict__ cb_out, float *__restrict__ qn_out) {
     constexpr int NC = PROBER_CAND, H = PROBER_HIDDEN;
     static_assert(H == 256 && NC == 64, "warp-per-row MLP layout: 32 lanes x 8 weights, 8 warps x 8 candidates");
     __shared__ int32_t sc[NC];
@@ -1000,6 +1004,24 @@ __global__ void __launch_bounds__(256) coarse_probe_kernel(const float *__restri
         a = fmaf(sf[i], wv, a);
     }
     sh1[j] = fmaxf(a, 0.f);
+    if (h1_out) {
+        // batched MLP: hand the first layer, the candidates, their bounds and
+        // |q|^2 to mlp_probe_kernel, which runs layers 2 and 3 for 8 queries
+        // per block (W2 read once per 8 queries instead of once per query)
+        h1_out[q * H + j] = sh1[j];
+        if (j < NC) {
+            cand_out[q * NC + j] = sc[j];
+            cb_out[q * NC + j] = sb[j];
+        }
+        if (warp == 2) {
+            float qs = 0.f;
+            for (int t = lane; t < d; t += 32) qs = fmaf(sqr[t], sqr[t], qs);
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) qs += __shfl_xor_sync(0xffffffffu, qs, o);
+            if (lane == 0) qn_out[q] = qs;
+        }
+        return;
+    }
     __syncthreads();
     // layer 2: warp w computes outputs 32w .. 32w + 31, one W2 row (512 bytes,
     // lane l its 16 bytes) per load instruction, four rows in flight; lane l
@@ -1096,6 +1118,135 @@ __global__ void __launch_bounds__(256) coarse_probe_kernel(const float *__restri
     if (qbound) write_probe_bound(keep ? sb[i] : INFINITY, sqr, d, xmax, qbound, q, sred);
 }
 
+// Layers 2 and 3 of the prober and the probe choice for MLP_QB queries per
+// block (large batches; the first layer ran in coarse_probe_kernel):
+//   layer 2  thread j = hidden unit j for the block's queries, its W2 row
+//            read once (16-byte loads), the queries' first-layer outputs from
+//            shared memory;
+//   layer 3  warp w = query w: its 64 candidate lists' W3 rows (one 512-byte
+//            row per load instruction, four in flight) against the query's
+//            second-layer output;
+//   choice   the nearest candidate always, the others whose logit is at
+//            least the threshold, in distance order; the list scan's score
+//            bound from the chosen lists.
+// The arithmetic (FP32 accumulation of BF16 weights, same order per dot
+// product within a lane) matches the fused kernel's up to summation order.
+constexpr int MLP_QB = 8;
+constexpr int64_t MLP_BATCH_MIN = 1024;  // smaller batches keep the MLP fused in coarse_probe_kernel
+__global__ void __launch_bounds__(256) mlp_probe_kernel(const float *__restrict__ H1,
+                                                        const int32_t *__restrict__ cand,
+                                                        const float *__restrict__ cb, const float *__restrict__ qnv,
+                                                        int64_t nq, ProberWeights w, float logit_tau, float xmax,
+                                                        int32_t *__restrict__ probes, int32_t *__restrict__ nprobed,
+                                                        uint32_t *__restrict__ qbound) {
+    constexpr int NC = PROBER_CAND, H = PROBER_HIDDEN;
+    __shared__ __align__(16) float h1s[MLP_QB][H], h2s[MLP_QB][H];
+    const int j = threadIdx.x, lane = j & 31, warp = j >> 5;
+    const int64_t q0 = (int64_t)blockIdx.x * MLP_QB;
+    const int nqb = (int)min((int64_t)MLP_QB, nq - q0);
+    for (int i = j; i < MLP_QB * H; i += 256) {
+        const int qq = i / H;
+        h1s[qq][i % H] = qq < nqb ? H1[(q0 + qq) * H + i % H] : 0.f;
+    }
+    __syncthreads();
+    {   // layer 2
+        const __nv_bfloat16 *W2 = reinterpret_cast<const __nv_bfloat16 *>(w.W2);
+        const uint4 *row = reinterpret_cast<const uint4 *>(W2 + (size_t)j * H);
+        float acc[MLP_QB];
+#pragma unroll
+        for (int qq = 0; qq < MLP_QB; ++qq) acc[qq] = 0.f;
+#pragma unroll 4
+        for (int i8 = 0; i8 < H / 8; ++i8) {
+            const uint4 u = __ldg(row + i8);
+            const __nv_bfloat162 *h = reinterpret_cast<const __nv_bfloat162 *>(&u);
+            float wv[8];
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+                const float2 f = __bfloat1622float2(h[e]);
+                wv[2 * e] = f.x;
+                wv[2 * e + 1] = f.y;
+            }
+#pragma unroll
+            for (int qq = 0; qq < MLP_QB; ++qq) {
+                const float4 x0 = *reinterpret_cast<const float4 *>(&h1s[qq][8 * i8]);
+                const float4 x1 = *reinterpret_cast<const float4 *>(&h1s[qq][8 * i8 + 4]);
+                acc[qq] = fmaf(wv[0], x0.x, acc[qq]);
+                acc[qq] = fmaf(wv[1], x0.y, acc[qq]);
+                acc[qq] = fmaf(wv[2], x0.z, acc[qq]);
+                acc[qq] = fmaf(wv[3], x0.w, acc[qq]);
+                acc[qq] = fmaf(wv[4], x1.x, acc[qq]);
+                acc[qq] = fmaf(wv[5], x1.y, acc[qq]);
+                acc[qq] = fmaf(wv[6], x1.z, acc[qq]);
+                acc[qq] = fmaf(wv[7], x1.w, acc[qq]);
+            }
+        }
+        const float b2 = w.b2[j];
+#pragma unroll
+        for (int qq = 0; qq < MLP_QB; ++qq) h2s[qq][j] = fmaxf(acc[qq] + b2, 0.f);
+    }
+    __syncthreads();
+    if (warp >= nqb) return;
+    const int64_t q = q0 + warp;
+    // layer 3 for this warp's query: lane l holds h2[8l .. 8l + 7]
+    const __nv_bfloat16 *W3 = reinterpret_cast<const __nv_bfloat16 *>(w.W3);
+    const float4 x0 = *reinterpret_cast<const float4 *>(&h2s[warp][8 * lane]);
+    const float4 x1 = *reinterpret_cast<const float4 *>(&h2s[warp][8 * lane + 4]);
+    const float xs[8] = {x0.x, x0.y, x0.z, x0.w, x1.x, x1.y, x1.z, x1.w};
+    const int32_t c_lo = cand[q * NC + lane], c_hi = cand[q * NC + 32 + lane];
+    float z_lo = -INFINITY, z_hi = -INFINITY;
+#pragma unroll 1
+    for (int i0 = 0; i0 < NC; i0 += 4) {
+        uint4 u[4];
+        int cs[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            cs[k] = __shfl_sync(0xffffffffu, (i0 + k) < 32 ? c_lo : c_hi, (i0 + k) & 31);
+            u[k] = cs[k] >= 0 ? __ldg(reinterpret_cast<const uint4 *>(W3 + (size_t)cs[k] * H) + lane)
+                              : make_uint4(0u, 0u, 0u, 0u);
+        }
+        float acc[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const __nv_bfloat162 *h = reinterpret_cast<const __nv_bfloat162 *>(&u[k]);
+            float t = 0.f;
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+                const float2 f = __bfloat1622float2(h[e]);
+                t = fmaf(f.x, xs[2 * e], t);
+                t = fmaf(f.y, xs[2 * e + 1], t);
+            }
+            acc[k] = t;
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+            for (int k = 0; k < 4; ++k) acc[k] += __shfl_xor_sync(0xffffffffu, acc[k], o);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const int i = i0 + k;
+            const float z = cs[k] >= 0 ? acc[k] + w.b3[cs[k]] : -INFINITY;
+            if (i < 32 && lane == i) z_lo = z;
+            if (i >= 32 && lane == i - 32) z_hi = z;
+        }
+    }
+    // the choice: candidate 0 always, the others at or above the threshold
+    const bool k_lo = c_lo >= 0 && (lane == 0 || z_lo >= logit_tau);
+    const bool k_hi = c_hi >= 0 && z_hi >= logit_tau;
+    const unsigned m_lo = __ballot_sync(0xffffffffu, k_lo), m_hi = __ballot_sync(0xffffffffu, k_hi);
+    const int n_lo = __popc(m_lo);
+    if (k_lo) probes[q * NC + __popc(m_lo & ((1u << lane) - 1u))] = c_lo;
+    if (k_hi) probes[q * NC + n_lo + __popc(m_hi & ((1u << lane) - 1u))] = c_hi;
+    const int total = n_lo + __popc(m_hi);
+    for (int t = total + lane; t < NC; t += 32) probes[q * NC + t] = -1;
+    if (lane == 0 && nprobed) nprobed[q] = total;
+    if (qbound) {
+        float b = fminf(k_lo ? cb[q * NC + lane] : INFINITY, k_hi ? cb[q * NC + 32 + lane] : INFINITY);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) b = fminf(b, __shfl_xor_sync(0xffffffffu, b, o));
+        if (lane == 0) qbound[q] = probe_bound_key(b, qnv[q], xmax);
+    }
+}
+
 // Probes of the tensor-core engine: BF16 centroid scores on the tensor cores,
 // exact re-rank of the 64 best, then fixed n_probe or the learned prober.
 static int ivfl2_probes_tc(gn_index *ix, const float *dQ, int64_t nq, int *np_out, cudaStream_t st) {
@@ -1148,20 +1299,37 @@ static int ivfl2_probes_tc(gn_index *ix, const float *dQ, int64_t nq, int *np_ou
         GN_CUDA_TRY(cudaFuncSetAttribute(coarse_probe_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ksm));
     }
     ProberWeights w;
+    float *h1 = nullptr, *cbnd = nullptr, *qnv = nullptr;
+    int32_t *cand = nullptr;
     if (mlp) {
         GN_TRY(prober_weights(S.prober, &w));
         GN_TRY(T.nprobed.ensure((size_t)nq * 4));
+        if (nq >= MLP_BATCH_MIN) {  // layers 2 and 3 batched over 8 queries per block
+            GN_TRY(T.mh1.ensure((size_t)nq * PROBER_HIDDEN * 4));
+            GN_TRY(T.mcand.ensure((size_t)nq * PROBER_CAND * 4));
+            GN_TRY(T.mcb.ensure((size_t)nq * PROBER_CAND * 4));
+            GN_TRY(T.mqn.ensure((size_t)nq * 4));
+            h1 = T.mh1.as<float>();
+            cand = T.mcand.as<int32_t>();
+            cbnd = T.mcb.as<float>();
+            qnv = T.mqn.as<float>();
+        }
         coarse_probe_kernel<true><<<(unsigned)nq, 256, ksm, st>>>(S.cscores.as<float>(), S.nc, ncp2, dQ, S.d, S.dp,
                                                                S.cent.as<float>(), nq, np, w, S.prober_tau,
                                                                T.probes.as<int32_t>(), T.nprobed.as<int32_t>(),
                                                                S.rho.as<float>(), S.shortlist, S.xmax,
-                                                               T.qbound.as<uint32_t>());
+                                                               T.qbound.as<uint32_t>(), h1, cand, cbnd, qnv);
+        if (h1)
+            mlp_probe_kernel<<<(unsigned)ceil_div(nq, MLP_QB), 256, 0, st>>>(
+                h1, cand, cbnd, qnv, nq, w, S.prober_tau, S.xmax, T.probes.as<int32_t>(), T.nprobed.as<int32_t>(),
+                T.qbound.as<uint32_t>());
     } else {
         coarse_probe_kernel<false><<<(unsigned)nq, 256, ksm, st>>>(S.cscores.as<float>(), S.nc, ncp2, dQ, S.d, S.dp,
                                                                 S.cent.as<float>(), nq, np, w, 0.f,
                                                                 T.probes.as<int32_t>(), nullptr,
                                                                 S.rho.as<float>(), S.shortlist, S.xmax,
-                                                                T.qbound.as<uint32_t>());
+                                                                T.qbound.as<uint32_t>(), nullptr, nullptr, nullptr,
+                                                                nullptr);
     }
     GN_CUDA_TRY(cudaGetLastError());
     return GN_OK;

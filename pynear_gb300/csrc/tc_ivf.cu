@@ -87,6 +87,9 @@ __global__ void __launch_bounds__(TI_THREADS, 1)
     uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 2 * TI_STAGES + 2 * TI_NACC);
     uint64_t *ufull = bars + 2 * TI_STAGES + 2 * TI_NACC + 1, *uempty = ufull + TI_UR;
     volatile int64_t *uring = reinterpret_cast<volatile int64_t *>(uempty + TI_UR);
+    // the units' descriptors travel with their indices: the MMA and epilogue
+    // warps read them from shared memory, not from global memory at every unit
+    TcUnit *uunit = reinterpret_cast<TcUnit *>(const_cast<int64_t *>(uring + TI_UR));
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     volatile int *verr = err;
 
@@ -118,16 +121,25 @@ __global__ void __launch_bounds__(TI_THREADS, 1)
             uint32_t it = 0;
             bool ok = true;
             // units are taken dynamically (atomic counter): unit costs vary
-            // by orders of magnitude, a static split would leave SMs idle
+            // by orders of magnitude, a static split would leave SMs idle.
+            // The next unit is claimed and its descriptor loaded one unit
+            // ahead, so that neither round trip stalls the copies.
+            int64_t u_next = (int64_t)atomicAdd(next_unit, 1ull);
+            TcUnit un_next = {};
+            if (u_next < n_units) un_next = units[u_next];
             for (uint32_t ui = 0; ok; ++ui) {
                 const int r = ui % TI_UR;
                 if (!mbar_wait(uempty + r, ((ui / TI_UR) & 1) ^ 1, verr, wait_limit)) break;
-                int64_t u = (int64_t)atomicAdd(next_unit, 1ull);
-                if (u >= n_units) u = -1;
+                const int64_t u = u_next < n_units ? u_next : -1;
+                const TcUnit un = un_next;
+                if (u >= 0) {
+                    u_next = (int64_t)atomicAdd(next_unit, 1ull);
+                    if (u_next < n_units) un_next = units[u_next];
+                }
                 uring[r] = u;
+                uunit[r] = un;
                 mbar_arrive(ufull + r);
                 if (u < 0) break;
-                const TcUnit un = units[u];
                 const int nsel = ti_nsel(un.na);
                 const CUtensorMap *mq = nsel == 32 ? &tmQ32 : nsel == 64 ? &tmQ64 : &tmQ128;
                 const int ntile = (int)((un.r1 - un.r0 + TI_M - 1) / TI_M);
@@ -162,9 +174,9 @@ __global__ void __launch_bounds__(TI_THREADS, 1)
                 const int r = ui % TI_UR;
                 if (!mbar_wait(ufull + r, (ui / TI_UR) & 1, verr, wait_limit)) break;
                 const int64_t u = uring[r];
+                const TcUnit un = uunit[r];
                 mbar_arrive(uempty + r);
                 if (u < 0) break;
-                const TcUnit un = units[u];
                 const int nsel = ti_nsel(un.na);
                 const uint32_t idesc = idesc_bf16_f32(TI_M, nsel);
                 const int ntile = (int)((un.r1 - un.r0 + TI_M - 1) / TI_M);
@@ -211,10 +223,10 @@ __global__ void __launch_bounds__(TI_THREADS, 1)
             const int r = ui % TI_UR;
             if (!mbar_wait(ufull + r, (ui / TI_UR) & 1, verr, wait_limit)) break;
             const int64_t u = uring[r];
+            const TcUnit un = uunit[r];
             __syncwarp();
             if (lane == 0) mbar_arrive(uempty + r);
             if (u < 0) break;
-            const TcUnit un = units[u];
             const int nsel = ti_nsel(un.na);
             const int nchunk = nsel / 32;
             // segment base (aslot x seg_mul, minus the list start) and score

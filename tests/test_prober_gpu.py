@@ -81,3 +81,32 @@ def test_training_cuts_lists_scanned_at_fixed_recall(gn):
     ix.n_probe = fixed
     b, _, _ = ix.search_knn_arrays(held[:100], 10)
     assert np.array_equal(a, b)
+
+
+def test_batched_mlp_matches_fused_mlp(gn):
+    """Batches of 1,024 queries and more run the prober's layers 2 and 3 in a
+    separate kernel over eight queries per block; smaller batches keep them
+    fused in the probe kernel.  Both compute the same network (FP32 sums in a
+    different order), so the probe counts and the results agree except where a
+    logit sits at the threshold."""
+    db, q = _mixture(60_000, 48, 256, 3000, 5)
+    train = q[:1000]
+    ex = gn.FlatL2Index()
+    ex.set(db)
+    gt_train, _ = ex.search_knn_arrays(train, 10)
+    ix = gn.IVFFlatL2Index(n_clusters=192, n_probe=4, engine="tc")
+    ix.set(db)
+    pr = gn.LearnedProber(ix, seed=2)
+    pr.train(train, gt_train, epochs=3, batch=512, lr=2e-3)
+    ix.set_prober(pr, 0.2)
+    held = q[1000:]
+    big_i, big_d, big_c = ix.search_knn_arrays(held, 10)  # 2,000 queries: batched MLP
+    big_lists = ix.last_lists_probed(len(held)).copy()
+    sm_i, small_lists = [], []
+    for s in range(0, len(held), 500):  # 500-query batches: fused MLP
+        sm_i.append(ix.search_knn_arrays(held[s:s + 500], 10)[0])
+        small_lists.append(ix.last_lists_probed(500).copy())
+    sm_i, small_lists = np.concatenate(sm_i), np.concatenate(small_lists)
+    assert np.mean(big_lists == small_lists) >= 0.99
+    assert np.mean(np.all(big_i == sm_i, axis=1)) >= 0.99
+    assert big_lists.min() >= 1
