@@ -3,7 +3,9 @@
 //   0. probes  coarse_probe_kernel: BF16 centroid scores (tc_ivf_kernel over
 //              the centroids), radix select of the 64 best, exact FP32
 //              distances, then the first n_probe or the learned prober's
-//              choice (its MLP fused here);
+//              choice (its MLP fused here; from 1,024 queries its layers 2
+//              and 3 run in mlp_probe_kernel over 8 queries per block), and
+//              each query's score bound for the scan;
 //   1. plan    the same bucketing and work plan as the FP32 scan (ivf.cu),
 //              score segments in 128-row slots;
 //   2. Qb      the BF16 copy of each (query, probe) pair's query, rows grouped by
@@ -11,9 +13,10 @@
 //   3. units   one tensor-core work unit per (list, row chunk, 128-query chunk);
 //   4. scan    tc_ivf_kernel: BF16 tcgen05 GEMM of the list's rows (M = 128
 //              per tile) against the unit's queries (N = 32..128) with FP32
-//              accumulation; the score |x|^2 - 2 q.x (exact FP32 |x|^2) of
-//              every (pair, row) goes to the pair's slots, and the minimum of
-//              every 32-row quarter to the slot's four minima;
+//              accumulation; the minimum score |x|^2 - 2 q.x (exact FP32
+//              |x|^2) of every 32-row quarter goes to the slot's four minima,
+//              and the quarter's scores to the pair's slots when that minimum
+//              is within the query's bound;
 //   5. select  per query: a threshold from the quarter minima, only the
 //              quarters below it are read, the S best keys (S = shortlist) by
 //              radix select, their squared L2 recomputed exactly in FP32 with a
@@ -359,10 +362,11 @@ __device__ __forceinline__ void sel_buffer_offer(uint64_t key, bool want, uint64
 //              (radix select): S distinct rows score <= tau, so tau bounds the
 //              query's S-th best score; tau is capped by the query's bound
 //              from the probe stage, above which the scan stored no quarter;
-//   sweep      warps take 8 slots at a time (lane l: quarter l % 4 of slot
-//              l / 4) and load only the 32-row quarters whose minimum is
-//              <= tau (one coalesced 128-byte load each, four in flight) —
-//              typically a few dozen of the query's hundreds of slots;
+//   sweep      the quarters whose minimum is <= tau, listed from the minima
+//              staged for the threshold (typically a few dozen of the query's
+//              hundreds of slots), are read four per warp at a time (one
+//              coalesced 128-byte load each); slots beyond the staged ones are
+//              swept 8 at a time (lane l: quarter l % 4 of slot l / 4);
 //   buffer     scores <= tau become keys in the warp's shared-memory buffer
 //              (512 keys); a full buffer is sorted and cut to its best S;
 //   select     radix select of the S smallest keys of all warps' buffers;
