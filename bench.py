@@ -583,9 +583,9 @@ def bench_flat_l2(args, dist, clocks_mhz):
 # ── exact flat L2 at 1M x 128 (larger than L2): HBM-bound small batches ─────
 def bench_flat_l2_hbm(args, dist, peaks, clocks_mhz):
     """Exact flat L2 in the reference's arithmetic order over a database larger
-    than L2 (1,000,000 x 128 float32, 512 MB): with 8 queries per call the
-    scan streams the database once per call and is bound by HBM (reported in
-    GB/s of database read against the measured copy bandwidth); with 1,024
+    than L2 (1,000,000 x 128 float32, 512 MB): with 1 or 8 queries per call
+    the scan streams the database once per call and is bound by HBM (reported
+    in GB/s of database read against the measured copy bandwidth); with 1,024
     queries per call it is bound by the FP32 pipe (3 flops per element and
     query).  Indices checked against the oracle on a subset."""
     import torch
@@ -610,7 +610,7 @@ def bench_flat_l2_hbm(args, dist, peaks, clocks_mhz):
                       "l2": "database (512 MB) exceeds L2; no flush"}}
     import oracle
     oracle.build()
-    for nq in (8, 1024):
+    for nq in (1, 8, 1024):
         def step():
             _lib.check(lib.gn_flat_search_knn_device(ix._h.h, vp(d_q), nq, K, vp(d_idx), vp(d_dist),
                                                      ctypes.c_void_p(stream.cuda_stream)))
