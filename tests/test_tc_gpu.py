@@ -158,3 +158,34 @@ def test_tc_shortlist_full_size_1m_x128(gn, oracle):
     sub = 200
     d64 = np.sqrt(((q[:sub, None, :].astype(np.float64) - db[idx[:sub]].astype(np.float64)) ** 2).sum(-1))
     assert np.abs(dist[:sub] - d64).max() <= 1e-5 * d64.max()
+
+
+def test_ivf_tc_score_bound_filters_and_stays_exact(gn, oracle):
+    """Well separated clusters, one per list: the probe stage's score bound
+    (the shortlist-th nearest row of a probed list lies within |q - c| + rho
+    of the query) sits far below other clusters' rows, so the list scan stores
+    only the score quarters of each query's own cluster.  The results must be
+    the exact top-k of the probed lists all the same, for k up to the
+    shortlist and with queries far from every cluster (a loose bound)."""
+    rng = np.random.default_rng(43)
+    centres = np.float32(4.0) * rng.standard_normal((96, 128), dtype=np.float32)
+    comp = np.repeat(np.arange(96), 400)
+    data = (centres[comp] + np.float32(0.2) * rng.standard_normal((len(comp), 128), dtype=np.float32))
+    q_near = centres[rng.integers(0, 96, 300)] + np.float32(0.2) * rng.standard_normal((300, 128), dtype=np.float32)
+    q_far = np.float32(8.0) * rng.standard_normal((40, 128), dtype=np.float32)
+    q = np.concatenate([q_near, q_far]).astype(np.float32)
+    ix = gn.IVFFlatL2Index(n_clusters=96, n_probe=3, engine="tc")
+    ix.set(data)
+    cent, offs, ids = ix.export()
+    labels = np.empty(len(data), np.int32)
+    for c in range(len(offs) - 1):
+        labels[ids[offs[c]:offs[c + 1]]] = c
+    for k in (1, 10, 32):
+        idx, dist, cnt = ix.search_knn_arrays(q, k)
+        oi, od, oc = oracle.ivfl2_search(data, cent, labels, q, k, 3)
+        assert np.array_equal(cnt, oc), k
+        assert np.mean(idx == oi) >= 0.995, k
+        np.testing.assert_allclose(dist, od, rtol=1e-4, atol=1e-3)
+        d64 = ((q[:, None, :].astype(np.float64) - data[np.maximum(idx, 0)].astype(np.float64)) ** 2).sum(-1)
+        ok = idx >= 0
+        assert np.max(np.abs(dist[ok] - d64[ok]) / np.maximum(d64[ok], 1e-6)) < 1e-6
