@@ -92,7 +92,7 @@ int gn_index_size(gn_index *ix, int64_t *n, int64_t *dim);
  * The only other memory used is a fixed 16 MB array per device inside the
  * library, so nq * k must be at most 2 Mi (larger requests fail with
  * GN_ERR_INVALID); 1 <= k <= 256.  Set-up: the first call on a device loads
- * the library's scan kernels and that array (the driver loads modules lazily,
+ * the library's scan kernels and that array (the CUDA driver loads modules lazily,
  * and reserves their memory then) and looks up the array's address
  * (cudaGetSymbolAddress); make that first call (nq = 0 is enough) at set-up
  * time, with the device current and before any stream capture; later calls

@@ -3,7 +3,7 @@
 Wraps ``oracle.cpp`` (a C++ restatement of the reference's distance, k-NN,
 k-means and IVF routines; see the citations there) through ctypes.  Only the
 tests, ``__graft_entry__.smoke()`` and the CPU-baseline leg of ``bench.py`` use
-this package, always as the checker or the timed CPU baseline -- never as the
+this package, always as the expected answer or the timed CPU baseline -- never as the
 thing measured or shipped.
 """
 from __future__ import annotations

@@ -11,7 +11,7 @@
 //
 // Set-up: the library's kernels and this array live in modules that the CUDA
 // driver loads lazily (the default since CUDA 12.2), so the FIRST call on a
-// device loads them, and that load is when the driver reserves the array's
+// device loads them, and that load is when the CUDA driver reserves the array's
 // 16 MB and the kernels' code.  A caller that must not allocate later makes
 // one call at set-up time (nq = 0 is enough: it loads everything and scans
 // nothing), with that device current and before any stream capture.  After

@@ -1,5 +1,5 @@
 // tmap.cuh — 2-D TMA tensor maps (cuTensorMapEncodeTiled, resolved through the
-// runtime so that the library has no link-time dependency on the driver).
+// runtime so that the library has no link-time dependency on the CUDA driver library).
 #pragma once
 
 #include <cuda.h>

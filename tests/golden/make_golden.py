@@ -8,7 +8,7 @@ built its extension into oracle/_ref/:
 
 Every fixture stores seeded inputs plus the reference's own outputs for them,
 produced through its public Python API (the _pynear extension and the pynear
-package's IVFFlatL2Index).  The GPU machine has no reference tree; the tests there
+package's IVFFlatL2Index).  Machines without the reference tree (the GPU hosts)
 read only these committed .npz files.
 """
 from __future__ import annotations
