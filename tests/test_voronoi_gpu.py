@@ -110,3 +110,18 @@ def test_errors(gn):
         gn.voronoi_raster(np.zeros((3, 2), np.float32), 4, 4, palette=np.zeros((0, 4), np.uint8))
     with pytest.raises(ValueError):
         gn.voronoi_raster(np.zeros((3, 2), np.float32))
+
+
+def test_lattice_seeds_many_ties_against_oracle(gn, oracle):
+    """Seeds and pixels on lattices: many pixels are equally far from several
+    seeds (and from seeds that repeat), so the kernel's four-seed groups often
+    hold equal or nearly equal distances; ids (ties to the lower index) and
+    distance bits equal the oracle's."""
+    rng = np.random.default_rng(5)
+    seeds = (rng.integers(0, 33, (3001, 2)) / np.float32(32.0)).astype(np.float32)
+    xs = np.linspace(0, 1, 129, dtype=np.float32)
+    ys = np.linspace(0, 1, 65, dtype=np.float32)
+    r = gn.voronoi_raster(seeds, xs=xs, ys=ys, with_distance=True)
+    o_ids, o_dist = oracle.voronoi_raster(seeds, xs, ys)
+    assert np.array_equal(r.ids, o_ids)
+    assert np.array_equal(r.dist.view(np.uint32), o_dist.view(np.uint32))
