@@ -277,7 +277,21 @@ __global__ void flat_merge_kernel(const uint64_t *__restrict__ part, int n_slice
     L.init();
     uint64_t thr = KEY_EMPTY;
     const uint64_t *p = part + (size_t)qi * n_slices * k;
-    for (int s = 0; s < n_slices; ++s) {
+    if (k <= 32) {
+        // one 32-key chunk per slice: the chunks of MERGE_AHEAD slices are
+        // loaded together, so that a small batch's hundreds of slices cost
+        // hundreds / MERGE_AHEAD load latencies instead of one each
+        constexpr int MERGE_AHEAD = 16;
+        for (int s0 = 0; s0 < n_slices; s0 += MERGE_AHEAD) {
+            uint64_t kk[MERGE_AHEAD];
+#pragma unroll
+            for (int u = 0; u < MERGE_AHEAD; ++u)
+                kk[u] = (s0 + u < n_slices && lane < k) ? p[(size_t)(s0 + u) * k + lane] : KEY_EMPTY;
+#pragma unroll
+            for (int u = 0; u < MERGE_AHEAD; ++u)
+                if (!__all_sync(0xffffffffu, kk[u] >= thr)) L.offer(kk[u], thr, k);
+        }
+    } else for (int s = 0; s < n_slices; ++s) {
         for (int j0 = 0; j0 < k; j0 += 32) {
             int j = j0 + lane;
             uint64_t key = (j < k) ? p[(size_t)s * k + j] : KEY_EMPTY;
@@ -478,10 +492,15 @@ static int float_scan_occupancy(int metric, int qw, int threads, size_t smem) {
 void flat_plan(FlatScanArgs &a) {
     const DevInfo &di = dev_info();
     // float metrics: four queries per warp, fewer for a small batch with
-    // k <= 32 so that every warp scores real queries
+    // k <= 32 so that every warp scores real queries; and no more warps than
+    // the batch fills (every warp of a CTA reads each staged row block from
+    // shared memory, so a warp of padding queries takes shared-memory
+    // bandwidth from the scan: one query over 1M x 128 rows 0.131 -> 0.092 ms).
+    // More warps with fewer queries each beat fewer warps with more (4 queries:
+    // 4 warps of one 0.133 ms, 1 warp of four 0.167 ms).
     const int qw = (a.metric == M_HAMMING) ? 8 : (a.k <= 32 && a.nq <= 4) ? 1 : (a.k <= 32 && a.nq <= 8) ? 2 : 4;
     const size_t per_warp = (size_t)qw * a.stride4 * 16;
-    int warps = 4;
+    int warps = a.metric == M_HAMMING ? 4 : (int)std::min<int64_t>(4, std::max<int64_t>(1, ceil_div(a.nq, (int64_t)qw)));
     while (warps > 1 && per_warp * warps > 200 * 1024) warps >>= 1;
     a.warps = warps;
     a.qw = qw;

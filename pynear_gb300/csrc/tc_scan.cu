@@ -56,14 +56,15 @@ constexpr int TC_STAGE_BYTES = TC_A_BYTES + TC_B_BYTES;
 // its half; the halves merge at the end of a unit).
 __host__ __device__ constexpr int tc_nepi(int S) { return 8; }
 __host__ __device__ constexpr int tc_threads(int S) { return 64 + 32 * tc_nepi(S); }
-// pipeline depth: two stages when the lists of S = 40, 64 need the room
-__host__ __device__ constexpr int tc_stages(int S) { return S > 32 ? 2 : 3; }
+// pipeline depth: three stages, two where the lists need the room (S above
+// 40; S = 40 with FP8's column scales)
+__host__ __device__ constexpr int tc_stages(int S, bool f8 = false) { return S > 40 || (S > 32 && f8) ? 2 : 3; }
 
 __host__ __device__ constexpr size_t tc_smem_bytes(int S, bool f8 = false) {
     // S == 0 is the store mode: a 32x33 transpose tile per epilogue warp;
     // top-S mode: two lists (one per column half) of S keys per query row;
     // per epilogue warp 32 column norms (and, FP8, 32 column scales)
-    return 1024 /*alignment slack*/ + (size_t)tc_stages(S) * TC_STAGE_BYTES +
+    return 1024 /*alignment slack*/ + (size_t)tc_stages(S, f8) * TC_STAGE_BYTES +
            (S ? (size_t)2 * TC_M * S * 8 : (size_t)tc_nepi(S) * 32 * 33 * 4) +
            (size_t)tc_nepi(S) * 32 * 4 * (f8 ? 2 : 1) + 256;
 }
@@ -104,7 +105,7 @@ __global__ void __launch_bounds__(tc_threads(S), 1)
     static_assert(!(STORE && F8), "the store mode is BF16 only");
     constexpr int SL = STORE ? 1 : 2 * S;  // list keys per query row (two column halves)
     constexpr int NEPI = tc_nepi(S);
-    constexpr int TC_STAGES = tc_stages(S);
+    constexpr int TC_STAGES = tc_stages(S, F8);
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
     uint8_t *stage_base = smem;
@@ -450,6 +451,8 @@ int tc_topk_launch(const TcLaunch &a, cudaStream_t st) {
     auto launch = [&](auto SC, auto FC) -> int {
         constexpr int Sv = decltype(SC)::value;
         constexpr bool Fv = decltype(FC)::value;
+        // 227 KB of shared memory per block, less the kernel's static 32 bytes
+        static_assert(tc_smem_bytes(Sv, Fv) + 32 <= 227 * 1024, "shortlist stages and lists exceed shared memory");
         const size_t smem = tc_smem_bytes(Sv, Fv);
         GN_CUDA_TRY(cudaFuncSetAttribute(tc_topk_kernel<Sv, Fv>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)smem));

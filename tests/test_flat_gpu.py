@@ -222,17 +222,19 @@ def test_pickle_roundtrip(gn):
     assert ix2.searchKNN(q, 4) == a
 
 
-@pytest.mark.parametrize("nq", [1, 3, 4, 5, 8])
+@pytest.mark.parametrize("nq", [1, 2, 3, 4, 5, 8])
 def test_small_batches(gn, oracle, nq):
-    """Batches of at most 8 queries (the scan's one- and two-query-per-warp
-    layouts): every width up to 129, odd ones included, and k up to 32."""
+    """Batches of at most 8 queries (the scan's one- and two-warp CTAs with
+    one, two or four queries per warp, padding queries included): every
+    width up to 129, odd ones included, k up to 32 and one k above it (two
+    keys per lane)."""
     rng = np.random.default_rng(100 + nq)
     for d in (1, 5, 17, 32, 63, 64, 100, 128, 129):
         db = (rng.random((3000, d), dtype=np.float32) * 4 - 2)
         q = (rng.random((nq, d), dtype=np.float32) * 4 - 2)
         for metric in ("l2", "l1", "linf"):
             ix = _flat(gn, metric, db)
-            for k in (1, 7, 32):
+            for k in (1, 7, 32, 40):
                 idx, dist = ix.search_knn_arrays(q, k)
                 oi, od = oracle.knn_float(metric, db, q, k)
                 assert np.array_equal(idx, oi), (metric, d, k)
