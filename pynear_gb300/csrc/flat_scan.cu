@@ -7,7 +7,8 @@
 // lane l scores row base+l against all of them (the row stays in registers,
 // query words come from shared memory as broadcasts), then offers the keys to
 // the warp's register top-k lists.  Each (query, slice) writes its sorted k
-// keys to a partial buffer; flat_merge_kernel reduces the slices.
+// keys to a partial buffer; flat_merge_kernel (flat_merge_split_kernel for
+// small batches) reduces the slices.
 //
 // Reference semantics (pynear/include/VPTree.hpp:143-191): exact k nearest rows
 // per query; here ties go to the lower row index.
@@ -265,42 +266,32 @@ __global__ void __launch_bounds__(128) float_scan_kernel(const __grid_constant__
 }
 
 // ── merge of per-slice partial lists → final output ───────────────────────
-// One warp per query.  Output: idx (int64, -1 for empty), dist as float32
+// Offer a query's sorted per-slice lists s_begin, s_begin + s_step, ... (k <=
+// 32: one 32-key chunk per slice) to a warp's list: the chunks of MERGE_AHEAD
+// slices are loaded together, so that a small batch's hundreds of slices cost
+// hundreds / MERGE_AHEAD load latencies instead of one each.
+constexpr int MERGE_AHEAD = 16;
+template <int R>
+__device__ __forceinline__ void merge_slices_ahead(const uint64_t *__restrict__ p, int s_begin, int n_slices,
+                                                   int s_step, int k, int lane, WarpTopK<R> &L, uint64_t &thr) {
+    for (int s0 = s_begin; s0 < n_slices; s0 += MERGE_AHEAD * s_step) {
+        uint64_t kk[MERGE_AHEAD];
+#pragma unroll
+        for (int u = 0; u < MERGE_AHEAD; ++u) {
+            const int s = s0 + u * s_step;
+            kk[u] = (s < n_slices && lane < k) ? p[(size_t)s * k + lane] : KEY_EMPTY;
+        }
+#pragma unroll
+        for (int u = 0; u < MERGE_AHEAD; ++u)
+            if (!__all_sync(0xffffffffu, kk[u] >= thr)) L.offer(kk[u], thr, k);
+    }
+}
+
+// Write a query's k nearest: idx (int64, -1 for empty), dist as float32
 // (float metrics) or int64 (Hamming).
 template <int R>
-__global__ void flat_merge_kernel(const uint64_t *__restrict__ part, int n_slices, int k, int64_t nq, int is_hamming,
-                                  int64_t *__restrict__ out_idx, void *__restrict__ out_dist) {
-    const int lane = threadIdx.x & 31;
-    const int64_t qi = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-    if (qi >= nq) return;
-    WarpTopK<R> L;
-    L.init();
-    uint64_t thr = KEY_EMPTY;
-    const uint64_t *p = part + (size_t)qi * n_slices * k;
-    if (k <= 32) {
-        // one 32-key chunk per slice: the chunks of MERGE_AHEAD slices are
-        // loaded together, so that a small batch's hundreds of slices cost
-        // hundreds / MERGE_AHEAD load latencies instead of one each
-        constexpr int MERGE_AHEAD = 16;
-        for (int s0 = 0; s0 < n_slices; s0 += MERGE_AHEAD) {
-            uint64_t kk[MERGE_AHEAD];
-#pragma unroll
-            for (int u = 0; u < MERGE_AHEAD; ++u)
-                kk[u] = (s0 + u < n_slices && lane < k) ? p[(size_t)(s0 + u) * k + lane] : KEY_EMPTY;
-#pragma unroll
-            for (int u = 0; u < MERGE_AHEAD; ++u)
-                if (!__all_sync(0xffffffffu, kk[u] >= thr)) L.offer(kk[u], thr, k);
-        }
-    } else for (int s = 0; s < n_slices; ++s) {
-        for (int j0 = 0; j0 < k; j0 += 32) {
-            int j = j0 + lane;
-            uint64_t key = (j < k) ? p[(size_t)s * k + j] : KEY_EMPTY;
-            // partial lists are sorted: once the smallest unseen key of this
-            // chunk is above the threshold the rest of the list is too
-            if (__all_sync(0xffffffffu, key >= thr)) break;
-            L.offer(key, thr, k);
-        }
-    }
+__device__ __forceinline__ void merge_store(const WarpTopK<R> &L, int64_t qi, int k, int is_hamming, int lane,
+                                            int64_t *__restrict__ out_idx, void *__restrict__ out_dist) {
 #pragma unroll
     for (int r = 0; r < R; ++r) {
         int pos = r * 32 + lane;
@@ -312,6 +303,58 @@ __global__ void flat_merge_kernel(const uint64_t *__restrict__ part, int n_slice
             else reinterpret_cast<float *>(out_dist)[qi * k + pos] = e ? 0.f : __uint_as_float(key_dist(key));
         }
     }
+}
+
+// One warp per query.
+template <int R>
+__global__ void flat_merge_kernel(const uint64_t *__restrict__ part, int n_slices, int k, int64_t nq, int is_hamming,
+                                  int64_t *__restrict__ out_idx, void *__restrict__ out_dist) {
+    const int lane = threadIdx.x & 31;
+    const int64_t qi = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (qi >= nq) return;
+    WarpTopK<R> L;
+    L.init();
+    uint64_t thr = KEY_EMPTY;
+    const uint64_t *p = part + (size_t)qi * n_slices * k;
+    if (k <= 32) merge_slices_ahead(p, 0, n_slices, 1, k, lane, L, thr);
+    else for (int s = 0; s < n_slices; ++s) {
+        for (int j0 = 0; j0 < k; j0 += 32) {
+            int j = j0 + lane;
+            uint64_t key = (j < k) ? p[(size_t)s * k + j] : KEY_EMPTY;
+            // partial lists are sorted: once the smallest unseen key of this
+            // chunk is above the threshold the rest of the list is too
+            if (__all_sync(0xffffffffu, key >= thr)) break;
+            L.offer(key, thr, k);
+        }
+    }
+    merge_store(L, qi, k, is_hamming, lane, out_idx, out_dist);
+}
+
+// Small batches (k <= 32): one block of MERGE_WARPS warps per query, so that
+// a batch too small to fill the GPU with one warp per query still merges its
+// hundreds of slices quickly: warp w takes slices w, w + MERGE_WARPS, ...,
+// then warp 0 offers the other warps' first k keys (disjoint rows) to its own
+// list.  The k nearest are the same keys in the same order as flat_merge_kernel's.
+constexpr int MERGE_WARPS = 8;
+__global__ void __launch_bounds__(MERGE_WARPS * 32)
+    flat_merge_split_kernel(const uint64_t *__restrict__ part, int n_slices, int k, int is_hamming,
+                            int64_t *__restrict__ out_idx, void *__restrict__ out_dist) {
+    __shared__ uint64_t wl[MERGE_WARPS][32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int64_t qi = blockIdx.x;
+    WarpTopK<1> L;
+    L.init();
+    uint64_t thr = KEY_EMPTY;
+    merge_slices_ahead(part + (size_t)qi * n_slices * k, warp, n_slices, MERGE_WARPS, k, lane, L, thr);
+    wl[warp][lane] = lane < k ? L.v[0] : KEY_EMPTY;
+    __syncthreads();
+    if (warp != 0) return;
+#pragma unroll 1
+    for (int w = 1; w < MERGE_WARPS; ++w) {
+        const uint64_t key = wl[w][lane];
+        if (!__all_sync(0xffffffffu, key >= thr)) L.offer(key, thr, k);
+    }
+    merge_store(L, qi, k, is_hamming, lane, out_idx, out_dist);
 }
 
 // ── large-k path: materialised keys + radix select + bitonic sort ────────
@@ -453,6 +496,12 @@ static int launch_scan(const FlatScanArgs &a, int n_groups, int threads, size_t 
         else if (a.metric == M_L1) by_qw(std::integral_constant<int, M_L1>());
         else by_qw(std::integral_constant<int, M_LINF>());
         timing_end(st);
+    }
+    // a batch of up to two queries per SM over many slices: a block per query
+    if (R == 1 && a.nq > 0 && a.nq <= 2 * dev_info().num_sms && a.n_slices >= 2 * MERGE_WARPS) {
+        flat_merge_split_kernel<<<(unsigned)a.nq, MERGE_WARPS * 32, 0, st>>>(
+            part, a.n_slices, a.k, a.metric == M_HAMMING, a.out_idx, a.out_dist);
+        return GN_OK;
     }
     const int qpb = 4;  // queries (warps) per merge block
     flat_merge_kernel<R><<<(unsigned)ceil_div(a.nq, qpb), qpb * 32, 0, st>>>(
@@ -598,7 +647,8 @@ int flat_preload_hamming() {
     const void *fns[] = {(const void *)hamming_scan_kernel<8, 1>, (const void *)hamming_scan_kernel<8, 2>,
                          (const void *)hamming_scan_kernel<8, 4>, (const void *)hamming_scan_kernel<8, 8>,
                          (const void *)flat_merge_kernel<1>,      (const void *)flat_merge_kernel<2>,
-                         (const void *)flat_merge_kernel<4>,      (const void *)flat_merge_kernel<8>};
+                         (const void *)flat_merge_kernel<4>,      (const void *)flat_merge_kernel<8>,
+                         (const void *)flat_merge_split_kernel};
     for (const void *f : fns) GN_CUDA_TRY(cudaFuncGetAttributes(&fa, f));
     return GN_OK;
 }
