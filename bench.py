@@ -1060,8 +1060,8 @@ def run_reference(args):
 
 
 # ── small profiling cases (one profiler region around exactly one call) ─────
-PROFILE_CASES = ("ivf_scan", "ivf_mlp", "ivf_1m", "ivf_step", "tc_shortlist", "flat_l2", "flat_l2_hbm", "hamming",
-                 "voronoi")
+PROFILE_CASES = ("ivf_scan", "ivf_mlp", "ivf_1m", "ivf_step", "tc_shortlist", "flat_l2", "flat_l2_hbm",
+                 "flat_l2_hbm_q1", "hamming", "voronoi")
 
 
 def profile_case(name):
@@ -1091,6 +1091,7 @@ def profile_case(name):
                     (the benchmark's shortlist step, about 1 GB on the device);
       flat_l2       exact flat L2, 100,000 x 32 uniform, 1,000 queries, k 5;
       flat_l2_hbm   exact flat L2, 1,000,000 x 128 FP32, 8 queries;
+      flat_l2_hbm_q1  the same database, 1 query;
       hamming       exact Hamming, 1,000,000 x 512 bits, 10,000 queries;
       voronoi       3840 x 2160 raster, 4,096 seeds.
     Prints one JSON line with the call's CUDA-event time (outside the region)."""
@@ -1158,10 +1159,10 @@ def profile_case(name):
         def call():
             _lib.check(lib.gn_flat_search_knn_device(ix._h.h, vp(d_q), len(q), 5, vp(o[0]), vp(o[1]),
                                                      ctypes.c_void_p(stream.cuda_stream)))
-    elif name == "flat_l2_hbm":
+    elif name in ("flat_l2_hbm", "flat_l2_hbm_q1"):
         rng = np.random.default_rng(17)
         db = rng.standard_normal((1_000_000, 128), dtype=np.float32)
-        q = rng.standard_normal((8, 128), dtype=np.float32)
+        q = rng.standard_normal((8, 128), dtype=np.float32)[: 1 if name == "flat_l2_hbm_q1" else 8]
         ix = gn.FlatL2Index()
         ix.set(db)
         d_q = torch.from_numpy(q).to(dev)
