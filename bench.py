@@ -643,6 +643,7 @@ def bench_flat_l2_hbm(args, dist, peaks, clocks_mhz):
         if nq <= 8:
             entry["roofline"] = {"bound": "hbm", "kernel": "float_scan_kernel", "achieved": gbs, "peak": hbm_peak,
                                  "unit": "GB/s", "frac": gbs / hbm_peak,
+                                 "traffic": profile_traffic(f"float_scan_kernel_q{nq}"),
                                  "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)",
                                  "algorithmic_per_launch": {"bytes": int(db.nbytes)}}
         else:
