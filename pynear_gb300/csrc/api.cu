@@ -95,6 +95,23 @@ int make_stream(gn_index *ix) {
     return GN_OK;
 }
 
+int finish_blocking(gn_index *ix, int *d_err, cudaStream_t st, const char *what) {
+    int *h = nullptr;
+    if (d_err) {
+        GN_TRY(ix->hstatus.ensure(sizeof(int)));
+        h = static_cast<int *>(ix->hstatus.p);
+        *h = 0;  // no copy into it is pending: every blocking search ends synchronised
+        GN_CUDA_TRY(cudaMemcpyAsync(h, d_err, sizeof(int), cudaMemcpyDeviceToHost, st));
+    }
+    GN_CUDA_TRY(cudaStreamSynchronize(st));
+    if (h && *h) {
+        GN_CUDA_TRY(cudaMemsetAsync(d_err, 0, sizeof(int), st));
+        GN_CUDA_TRY(cudaStreamSynchronize(st));
+        return fail(GN_ERR_TIMEOUT, what);
+    }
+    return GN_OK;
+}
+
 int upload_rows(DBuf &dst, const void *src, int64_t n, int64_t row_bytes, int stride4, cudaStream_t st,
                 bool src_on_device) {
     const size_t pitch = (size_t)stride4 * 16;
@@ -268,16 +285,9 @@ int gn_flat_search_knn(gn_index *ix, const void *queries, int64_t nq, int64_t k,
     const size_t dist_bytes = (size_t)nq * k * (ix->metric == GN_METRIC_HAMMING ? 8 : 4);
     GN_CUDA_TRY(cudaMemcpyAsync(out_idx, ix->out_idx.p, (size_t)nq * k * 8, cudaMemcpyDeviceToHost, st));
     GN_CUDA_TRY(cudaMemcpyAsync(out_dist, ix->out_dist.p, dist_bytes, cudaMemcpyDeviceToHost, st));
-    GN_CUDA_TRY(cudaStreamSynchronize(st));
-    if (ix->err.p) {  // a float scan's pipeline wait that ran out (reported once, then cleared)
-        int herr = 0;
-        GN_CUDA_TRY(cudaMemcpy(&herr, ix->err.p, 4, cudaMemcpyDeviceToHost));
-        if (herr) {
-            GN_CUDA_TRY(cudaMemset(ix->err.p, 0, 4));
-            return fail(GN_ERR_TIMEOUT, "flat scan: a pipeline wait timed out; results are invalid");
-        }
-    }
-    return GN_OK;
+    // a float scan's pipeline wait that ran out (reported once, then cleared)
+    return finish_blocking(ix, ix->err.p ? ix->err.as<int>() : nullptr, st,
+                           "flat scan: a pipeline wait timed out; results are invalid");
 }
 
 int gn_flat_search_1nn(gn_index *ix, const void *queries, int64_t nq, int64_t *out_idx, void *out_dist) {

@@ -62,6 +62,7 @@ struct gn_index {
     // per-call scratch (reused across calls)
     gn::DBuf q, part, out_idx, out_dist, keys, sorted;
     gn::DBuf err;         // float flat scans: error word of their bounded pipeline waits
+    gn::HBuf hstatus;     // pinned: a blocking search's error word, copied behind its results
     // kind-specific state
     gn::IvfL2State *ivfl2 = nullptr;
     gn::IvfBinState *ivfbin = nullptr;
@@ -80,6 +81,11 @@ struct gn_index {
 namespace gn {
 
 int make_stream(gn_index *ix);
+// End of a blocking search on stream st: the device error word d_err (may be
+// null) is copied into the index's pinned status word behind the results'
+// copies, the stream is synchronised once, and a pipeline wait that ran out
+// is reported as GN_ERR_TIMEOUT with message `what` (the word is cleared).
+int finish_blocking(gn_index *ix, int *d_err, cudaStream_t st, const char *what);
 // Register a new fork of `parent` / ask whether an index has live forks
 // (under the fork mutex).
 void fork_attach(gn_index *child, gn_index *parent);

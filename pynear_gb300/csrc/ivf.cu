@@ -895,14 +895,12 @@ using namespace gn;
 
 // After a synchronised search: a tensor-core pipeline wait that ran out set
 // the index's error word; report it (and clear it, so the next search runs).
-static int ivfl2_take_error(IvfL2State &S, cudaStream_t st) {
-    if (S.mode != 1 || !S.err.p) return GN_OK;
-    GN_CUDA_TRY(cudaStreamSynchronize(st));
-    int herr = 0;
-    GN_CUDA_TRY(cudaMemcpy(&herr, S.err.p, 4, cudaMemcpyDeviceToHost));
-    if (!herr) return GN_OK;
-    GN_CUDA_TRY(cudaMemset(S.err.p, 0, 4));
-    return fail(GN_ERR_TIMEOUT, "tensor-core IVF search: a pipeline wait timed out; results are invalid");
+// End of a blocking search: one stream synchronisation for the results and the
+// tensor-core engine's error word.
+static int ivfl2_finish(gn_index *ix, cudaStream_t st) {
+    IvfL2State &S = *ix->ivfl2;
+    return finish_blocking(ix, (S.mode == 1 && S.err.p) ? S.err.as<int>() : nullptr, st,
+                           "tensor-core IVF search: a pipeline wait timed out; results are invalid");
 }
 
 extern "C" {
@@ -1105,7 +1103,7 @@ int gn_ivfl2_search_knn(gn_index *ix, const float *queries, int64_t nq, int64_t 
     if (nq == 0) return GN_OK;
     if (S.graphs && nq <= S.graphs->max_batch && k == S.graphs->k && !timing_on() && !S.drill) {
         GN_TRY(ivfl2_search_graph(ix, queries, true, nq, (int)k, out_idx, out_dist, out_cnt, true, ix->stream));
-        return ivfl2_take_error(S, ix->stream);
+        return ivfl2_finish(ix, ix->stream);
     }
     cudaStream_t st = ix->stream;
     GN_TRY(upload_rows(S.s.q, queries, nq, S.d * 4, S.dp / 4, st));
@@ -1117,9 +1115,8 @@ int gn_ivfl2_search_knn(gn_index *ix, const float *queries, int64_t nq, int64_t 
     GN_CUDA_TRY(cudaMemcpyAsync(out_idx, ix->out_idx.p, (size_t)nq * k * 8, cudaMemcpyDeviceToHost, st));
     GN_CUDA_TRY(cudaMemcpyAsync(out_dist, ix->out_dist.p, (size_t)nq * k * 4, cudaMemcpyDeviceToHost, st));
     GN_CUDA_TRY(cudaMemcpyAsync(out_cnt, ix->part.p, (size_t)nq * 8, cudaMemcpyDeviceToHost, st));
-    GN_CUDA_TRY(cudaStreamSynchronize(st));
     GN_CUDA_TRY(cudaGetLastError());
-    return ivfl2_take_error(S, st);
+    return ivfl2_finish(ix, st);
 }
 
 int gn_ivfl2_set_n_probe(gn_index *ix, int32_t n_probe) {

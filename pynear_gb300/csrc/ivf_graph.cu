@@ -112,9 +112,9 @@ int ivfl2_search_graph(gn_index *ix, const float *q, bool q_host, int64_t nq, in
     GN_CUDA_TRY(cudaMemcpyAsync(idx, G.gidx.p, (size_t)nq * k * 8, kout, st));
     GN_CUDA_TRY(cudaMemcpyAsync(dist, G.gdist.p, (size_t)nq * k * 4, kout, st));
     GN_CUDA_TRY(cudaMemcpyAsync(cnt, G.gcnt.p, (size_t)nq * 8, kout, st));
-    if (out_host) {
-        GN_CUDA_TRY(cudaStreamSynchronize(st));
-    } else if (user != st) {
+    // host results: the caller synchronises the index's stream (with the
+    // error word's copy behind the results')
+    if (!out_host && user != st) {
         GN_CUDA_TRY(cudaEventRecord(G.ev_out, st));
         GN_CUDA_TRY(cudaStreamWaitEvent(user, G.ev_out, 0));
     }

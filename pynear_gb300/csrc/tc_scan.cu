@@ -791,14 +791,7 @@ int gn_tcflat_search_knn(gn_index *ix, const float *queries, int64_t nq, int64_t
                                        st));
     GN_CUDA_TRY(cudaMemcpyAsync(out_idx, S.out_idx.p, (size_t)nq * k * 8, cudaMemcpyDeviceToHost, st));
     GN_CUDA_TRY(cudaMemcpyAsync(out_dist, S.out_dist.p, (size_t)nq * k * 4, cudaMemcpyDeviceToHost, st));
-    GN_CUDA_TRY(cudaStreamSynchronize(st));
-    int herr = 0;
-    GN_CUDA_TRY(cudaMemcpy(&herr, S.err.p, 4, cudaMemcpyDeviceToHost));
-    if (herr) {
-        cudaMemset(S.err.p, 0, 4);
-        return fail(GN_ERR_TIMEOUT, "tensor-core scan: a pipeline wait timed out");
-    }
-    return GN_OK;
+    return finish_blocking(ix, S.err.as<int>(), st, "tensor-core scan: a pipeline wait timed out");
 }
 
 int gn_tcflat_set_precision(gn_index *ix, int32_t precision) {
