@@ -95,6 +95,55 @@ int make_stream(gn_index *ix) {
     return GN_OK;
 }
 
+// Page-locked host memory (allocated or registered with CUDA)?
+static bool host_pinned(const void *p) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeHost;
+}
+
+void begin_blocking(gn_index *ix) {
+    ix->pending.clear();
+    ix->pending_bytes = 0;
+}
+
+int stage_queries(gn_index *ix, const void *src, size_t bytes, cudaStream_t st, const void **out) {
+    *out = src;
+    if (bytes == 0 || bytes > STAGE_BYTES || host_pinned(src)) return GN_OK;
+    GN_TRY(ix->stage_in.ensure(STAGE_BYTES));  // one fixed size: never reallocated under a queued copy
+    // a search that ended early (an error) may have left a copy from it queued
+    if (ix->stage_in_busy) GN_CUDA_TRY(cudaStreamSynchronize(st));
+    std::memcpy(ix->stage_in.p, src, bytes);
+    ix->stage_in_busy = true;
+    *out = ix->stage_in.p;
+    return GN_OK;
+}
+
+int upload_queries(gn_index *ix, DBuf &dst, const void *src, int64_t n, int64_t row_bytes, int stride4,
+                   cudaStream_t st) {
+    const void *s = src;
+    if (n > 0) GN_TRY(stage_queries(ix, src, (size_t)n * (size_t)row_bytes, st, &s));
+    return upload_rows(dst, s, n, row_bytes, stride4, st);
+}
+
+int download_result(gn_index *ix, void *dst, const void *dsrc, size_t bytes, cudaStream_t st) {
+    if (bytes == 0) return GN_OK;
+    const size_t off = ix->pending_bytes, span = (bytes + 255) & ~(size_t)255;
+    if (off + span <= STAGE_BYTES && !host_pinned(dst)) {
+        GN_TRY(ix->stage_out.ensure(STAGE_BYTES));
+        GN_CUDA_TRY(cudaMemcpyAsync(static_cast<char *>(ix->stage_out.p) + off, dsrc, bytes, cudaMemcpyDeviceToHost,
+                                    st));
+        ix->pending.push_back({dst, off, bytes});
+        ix->pending_bytes = off + span;
+        return GN_OK;
+    }
+    GN_CUDA_TRY(cudaMemcpyAsync(dst, dsrc, bytes, cudaMemcpyDeviceToHost, st));
+    return GN_OK;
+}
+
 int finish_blocking(gn_index *ix, int *d_err, cudaStream_t st, const char *what) {
     int *h = nullptr;
     if (d_err) {
@@ -103,7 +152,15 @@ int finish_blocking(gn_index *ix, int *d_err, cudaStream_t st, const char *what)
         *h = 0;  // no copy into it is pending: every blocking search ends synchronised
         GN_CUDA_TRY(cudaMemcpyAsync(h, d_err, sizeof(int), cudaMemcpyDeviceToHost, st));
     }
-    GN_CUDA_TRY(cudaStreamSynchronize(st));
+    const cudaError_t se = cudaStreamSynchronize(st);
+    if (ix->stage_in_busy) ix->stage_in_busy = false;
+    if (!ix->pending.empty()) {  // (the entry points that stage hold the index's lock throughout)
+        if (se == cudaSuccess)
+            for (const auto &pd : ix->pending)
+                std::memcpy(pd.dst, static_cast<const char *>(ix->stage_out.p) + pd.off, pd.bytes);
+        begin_blocking(ix);
+    }
+    GN_CUDA_TRY(se);
     if (h && *h) {
         GN_CUDA_TRY(cudaMemsetAsync(d_err, 0, sizeof(int), st));
         GN_CUDA_TRY(cudaStreamSynchronize(st));
@@ -277,14 +334,15 @@ int gn_flat_search_knn(gn_index *ix, const void *queries, int64_t nq, int64_t k,
     std::lock_guard<std::mutex> lk(ix->mu);
     if (nq == 0) return GN_OK;
     cudaStream_t st = ix->stream;
+    begin_blocking(ix);
     const int64_t row_bytes = (ix->metric == GN_METRIC_HAMMING) ? ix->dim : ix->dim * 4;
-    GN_TRY(upload_rows(ix->q, queries, nq, row_bytes, ix->stride4, st));
+    GN_TRY(upload_queries(ix, ix->q, queries, nq, row_bytes, ix->stride4, st));
     GN_TRY(ix->out_idx.ensure((size_t)nq * k * 8));
     GN_TRY(ix->out_dist.ensure((size_t)nq * k * 8));
     GN_TRY(flat_search_dev(ix, ix->q.p, nq, k, ix->out_idx.as<int64_t>(), ix->out_dist.p, st));
     const size_t dist_bytes = (size_t)nq * k * (ix->metric == GN_METRIC_HAMMING ? 8 : 4);
-    GN_CUDA_TRY(cudaMemcpyAsync(out_idx, ix->out_idx.p, (size_t)nq * k * 8, cudaMemcpyDeviceToHost, st));
-    GN_CUDA_TRY(cudaMemcpyAsync(out_dist, ix->out_dist.p, dist_bytes, cudaMemcpyDeviceToHost, st));
+    GN_TRY(download_result(ix, out_idx, ix->out_idx.p, (size_t)nq * k * 8, st));
+    GN_TRY(download_result(ix, out_dist, ix->out_dist.p, dist_bytes, st));
     // a float scan's pipeline wait that ran out (reported once, then cleared)
     return finish_blocking(ix, ix->err.p ? ix->err.as<int>() : nullptr, st,
                            "flat scan: a pipeline wait timed out; results are invalid");

@@ -554,7 +554,9 @@ void flat_plan(FlatScanArgs &a) {
     a.warps = warps;
     a.qw = qw;
     const int64_t n_groups = ceil_div(a.nq, (int64_t)warps * qw);
-    const int64_t max_slices = std::max<int64_t>(1, a.n / 512);  // slices of at least 512 rows
+    // slices of at least 128 rows (one float stage): a small database spreads
+    // over more SMs instead of running a few CTAs through many stages
+    const int64_t max_slices = std::max<int64_t>(1, a.n / 128);
     int64_t slices;
     if (a.metric == M_HAMMING) {
         // aim for ~16 CTAs per SM over the launch

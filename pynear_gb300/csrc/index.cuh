@@ -63,6 +63,16 @@ struct gn_index {
     gn::DBuf q, part, out_idx, out_dist, keys, sorted;
     gn::DBuf err;         // float flat scans: error word of their bounded pipeline waits
     gn::HBuf hstatus;     // pinned: a blocking search's error word, copied behind its results
+    // pinned staging of a blocking search's small pageable copies (queries in,
+    // results out); staged results reach the caller's buffers after the sync
+    gn::HBuf stage_in, stage_out;
+    struct Pending {
+        void *dst;
+        size_t off, bytes;
+    };
+    std::vector<Pending> pending;
+    size_t pending_bytes = 0;
+    bool stage_in_busy = false;  // a copy from stage_in may still be queued
     // kind-specific state
     gn::IvfL2State *ivfl2 = nullptr;
     gn::IvfBinState *ivfbin = nullptr;
@@ -81,10 +91,28 @@ struct gn_index {
 namespace gn {
 
 int make_stream(gn_index *ix);
+// Blocking searches (the host-buffer entry points), in this order:
+// begin_blocking, then upload_queries / download_result for the caller's
+// buffers, then finish_blocking.  Pageable buffers of up to STAGE_BYTES go
+// through the index's pinned stage_in / stage_out, so that each copy is one
+// asynchronous DMA instead of the CUDA driver's staged pageable copy (about
+// 19 us of a 76 us one-query call measured); pinned or larger buffers are
+// copied directly.
+constexpr size_t STAGE_BYTES = (size_t)1 << 20;
+void begin_blocking(gn_index *ix);
+// Host -> device copy of n query rows in upload_rows' layout.
+int upload_queries(gn_index *ix, DBuf &dst, const void *src, int64_t n, int64_t row_bytes, int stride4,
+                   cudaStream_t st);
+// Host staging of query rows for a copy the caller issues: returns src, or
+// the pinned stage_in holding a copy of its `bytes`.
+int stage_queries(gn_index *ix, const void *src, size_t bytes, cudaStream_t st, const void **out);
+// Device -> host copy of `bytes` of results into the caller's dst.
+int download_result(gn_index *ix, void *dst, const void *dsrc, size_t bytes, cudaStream_t st);
 // End of a blocking search on stream st: the device error word d_err (may be
 // null) is copied into the index's pinned status word behind the results'
-// copies, the stream is synchronised once, and a pipeline wait that ran out
-// is reported as GN_ERR_TIMEOUT with message `what` (the word is cleared).
+// copies, the stream is synchronised once, staged results are copied to the
+// caller's buffers, and a pipeline wait that ran out is reported as
+// GN_ERR_TIMEOUT with message `what` (the word is cleared).
 int finish_blocking(gn_index *ix, int *d_err, cudaStream_t st, const char *what);
 // Register a new fork of `parent` / ask whether an index has live forks
 // (under the fork mutex).

@@ -1101,20 +1101,21 @@ int gn_ivfl2_search_knn(gn_index *ix, const float *queries, int64_t nq, int64_t 
         return fail(GN_ERR_INVALID, "bad query arguments");
     std::lock_guard<std::mutex> lk(ix->mu);
     if (nq == 0) return GN_OK;
+    begin_blocking(ix);
     if (S.graphs && nq <= S.graphs->max_batch && k == S.graphs->k && !timing_on() && !S.drill) {
         GN_TRY(ivfl2_search_graph(ix, queries, true, nq, (int)k, out_idx, out_dist, out_cnt, true, ix->stream));
         return ivfl2_finish(ix, ix->stream);
     }
     cudaStream_t st = ix->stream;
-    GN_TRY(upload_rows(S.s.q, queries, nq, S.d * 4, S.dp / 4, st));
+    GN_TRY(upload_queries(ix, S.s.q, queries, nq, S.d * 4, S.dp / 4, st));
     GN_TRY(ix->out_idx.ensure((size_t)nq * k * 8));
     GN_TRY(ix->out_dist.ensure((size_t)nq * k * 4));
     GN_TRY(ix->part.ensure((size_t)nq * 8));
     GN_TRY(ivfl2_search_core(ix, S.s.q.as<float>(), nq, (int)k, ix->out_idx.as<int64_t>(), ix->out_dist.as<float>(),
                             ix->part.as<int64_t>(), st));
-    GN_CUDA_TRY(cudaMemcpyAsync(out_idx, ix->out_idx.p, (size_t)nq * k * 8, cudaMemcpyDeviceToHost, st));
-    GN_CUDA_TRY(cudaMemcpyAsync(out_dist, ix->out_dist.p, (size_t)nq * k * 4, cudaMemcpyDeviceToHost, st));
-    GN_CUDA_TRY(cudaMemcpyAsync(out_cnt, ix->part.p, (size_t)nq * 8, cudaMemcpyDeviceToHost, st));
+    GN_TRY(download_result(ix, out_idx, ix->out_idx.p, (size_t)nq * k * 8, st));
+    GN_TRY(download_result(ix, out_dist, ix->out_dist.p, (size_t)nq * k * 4, st));
+    GN_TRY(download_result(ix, out_cnt, ix->part.p, (size_t)nq * 8, st));
     GN_CUDA_TRY(cudaGetLastError());
     return ivfl2_finish(ix, st);
 }
@@ -1237,16 +1238,17 @@ int gn_ivfbin_search_knn(gn_index *ix, const uint8_t *queries, int64_t nq, int64
         return GN_OK;
     }
     cudaStream_t st = ix->stream;
-    GN_TRY(upload_rows(S.s.q, queries, nq, S.nbytes, S.w4, st));
+    begin_blocking(ix);
+    GN_TRY(upload_queries(ix, S.s.q, queries, nq, S.nbytes, S.w4, st));
     GN_TRY(ix->out_idx.ensure((size_t)nq * k * 8));
     GN_TRY(ix->out_dist.ensure((size_t)nq * k * 8));
     GN_TRY(ix->part.ensure((size_t)nq * 8));
     GN_TRY(ivfbin_search_dev(ix, S.s.q.as<uint8_t>(), nq, (int)k, ix->out_idx.as<int64_t>(),
                              ix->out_dist.as<int64_t>(), ix->part.as<int64_t>(), st));
-    GN_CUDA_TRY(cudaMemcpyAsync(out_idx, ix->out_idx.p, (size_t)nq * k * 8, cudaMemcpyDeviceToHost, st));
-    GN_CUDA_TRY(cudaMemcpyAsync(out_dist, ix->out_dist.p, (size_t)nq * k * 8, cudaMemcpyDeviceToHost, st));
-    GN_CUDA_TRY(cudaMemcpyAsync(out_cnt, ix->part.p, (size_t)nq * 8, cudaMemcpyDeviceToHost, st));
-    GN_CUDA_TRY(cudaStreamSynchronize(st));
+    GN_TRY(download_result(ix, out_idx, ix->out_idx.p, (size_t)nq * k * 8, st));
+    GN_TRY(download_result(ix, out_dist, ix->out_dist.p, (size_t)nq * k * 8, st));
+    GN_TRY(download_result(ix, out_cnt, ix->part.p, (size_t)nq * 8, st));
+    GN_TRY(finish_blocking(ix, nullptr, st, ""));
     GN_CUDA_TRY(cudaGetLastError());
     return GN_OK;
 }

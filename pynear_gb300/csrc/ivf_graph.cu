@@ -79,6 +79,11 @@ int ivfl2_search_graph(gn_index *ix, const float *q, bool q_host, int64_t nq, in
     }
     // stage the queries at row pitch dp (the padding columns stay zero)
     const cudaMemcpyKind kin = q_host ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice;
+    if (q_host) {  // a small pageable batch goes through the index's pinned staging
+        const void *qs = q;
+        GN_TRY(stage_queries(ix, q, (size_t)nq * S.d * 4, st, &qs));
+        q = static_cast<const float *>(qs);
+    }
     if (S.d == S.dp)
         GN_CUDA_TRY(cudaMemcpyAsync(G.gq.p, q, (size_t)nq * S.d * 4, kin, st));
     else
@@ -108,10 +113,15 @@ int ivfl2_search_graph(gn_index *ix, const float *q, bool q_host, int64_t nq, in
             G.capture_failures++;
         }
     }
-    const cudaMemcpyKind kout = out_host ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
-    GN_CUDA_TRY(cudaMemcpyAsync(idx, G.gidx.p, (size_t)nq * k * 8, kout, st));
-    GN_CUDA_TRY(cudaMemcpyAsync(dist, G.gdist.p, (size_t)nq * k * 4, kout, st));
-    GN_CUDA_TRY(cudaMemcpyAsync(cnt, G.gcnt.p, (size_t)nq * 8, kout, st));
+    if (out_host) {
+        GN_TRY(download_result(ix, idx, G.gidx.p, (size_t)nq * k * 8, st));
+        GN_TRY(download_result(ix, dist, G.gdist.p, (size_t)nq * k * 4, st));
+        GN_TRY(download_result(ix, cnt, G.gcnt.p, (size_t)nq * 8, st));
+    } else {
+        GN_CUDA_TRY(cudaMemcpyAsync(idx, G.gidx.p, (size_t)nq * k * 8, cudaMemcpyDeviceToDevice, st));
+        GN_CUDA_TRY(cudaMemcpyAsync(dist, G.gdist.p, (size_t)nq * k * 4, cudaMemcpyDeviceToDevice, st));
+        GN_CUDA_TRY(cudaMemcpyAsync(cnt, G.gcnt.p, (size_t)nq * 8, cudaMemcpyDeviceToDevice, st));
+    }
     // host results: the caller synchronises the index's stream (with the
     // error word's copy behind the results')
     if (!out_host && user != st) {
