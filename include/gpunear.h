@@ -75,7 +75,11 @@ int gn_flat_create(int metric, gn_index **out);
 /* data: n rows of dim floats (float metrics) or dim bytes (Hamming); copied. */
 int gn_flat_set(gn_index *ix, const void *data, int64_t n, int64_t dim);
 /* out_idx: nq*k int64; out_dist: nq*k float32 (float metrics) or int64
- * (Hamming).  When k > n the trailing entries of each row are -1 / 0. */
+ * (Hamming).  When k > n the trailing entries of each row are -1 / 0.
+ * Host-buffer searches (this one, gn_ivfl2_search_knn, gn_ivfbin_search_knn,
+ * gn_tcflat_search_knn) block until the results are in the caller's buffers;
+ * they accept pageable or page-locked memory (pageable buffers of up to 1 MB
+ * are staged through the index's own page-locked buffers). */
 int gn_flat_search_knn(gn_index *ix, const void *queries, int64_t nq, int64_t k, int64_t *out_idx, void *out_dist);
 /* 1-NN shortcut (VPTree::search1NN, pynear/include/VPTree.hpp:169-191) */
 int gn_flat_search_1nn(gn_index *ix, const void *queries, int64_t nq, int64_t *out_idx, void *out_dist);
