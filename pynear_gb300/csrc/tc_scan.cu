@@ -724,15 +724,19 @@ int gn_tcflat_set(gn_index *ix, const float *data, int64_t n, int64_t d) {
     return GN_OK;
 }
 
-int gn_tcflat_search_knn_device(gn_index *ix, const float *d_queries, int64_t nq, int64_t k, int64_t *d_idx,
-                                float *d_dist, void *stream) {
+// Argument checks shared by the device- and host-buffer searches.
+static int tcflat_check(gn_index *ix, int64_t k) {
     if (!ix || ix->kind != K_TCFLAT) return fail(GN_ERR_INVALID, "not a tensor-core flat index");
     TcFlatState &S = *tcs(ix);
     if (S.n == 0) return fail(GN_ERR_EMPTY, "index is empty");
     if (k <= 0 || k > 32 || k > S.S) return fail(GN_ERR_INVALID, "k must be in [1, min(32, shortlist)]");
-    if (nq <= 0) return GN_OK;
-    std::lock_guard<std::mutex> lk(ix->mu);
-    cudaStream_t st = (cudaStream_t)stream;
+    return GN_OK;
+}
+
+// The search on device buffers, with the index's lock held by the caller.
+static int tcflat_search_locked(gn_index *ix, const float *d_queries, int64_t nq, int64_t k, int64_t *d_idx,
+                                float *d_dist, cudaStream_t st) {
+    TcFlatState &S = *tcs(ix);
     if (S.planned_nq != nq) GN_TRY(tcflat_plan(S, nq, st));
     GN_TRY(S.q16.ensure((size_t)std::max<int64_t>(nq, TC_M) * S.K * (S.fp8 ? 1 : 2)));  // >= one 128-row TMA box
     GN_TRY(S.part.ensure((size_t)nq * S.nchunks * S.S * 8));
@@ -773,24 +777,30 @@ int gn_tcflat_search_knn_device(gn_index *ix, const float *d_queries, int64_t nq
     return GN_OK;
 }
 
+int gn_tcflat_search_knn_device(gn_index *ix, const float *d_queries, int64_t nq, int64_t k, int64_t *d_idx,
+                                float *d_dist, void *stream) {
+    GN_TRY(tcflat_check(ix, k));
+    if (nq <= 0) return GN_OK;
+    std::lock_guard<std::mutex> lk(ix->mu);
+    return tcflat_search_locked(ix, d_queries, nq, k, d_idx, d_dist, (cudaStream_t)stream);
+}
+
 int gn_tcflat_search_knn(gn_index *ix, const float *queries, int64_t nq, int64_t k, int64_t *out_idx,
                          float *out_dist) {
-    if (!ix || ix->kind != K_TCFLAT) return fail(GN_ERR_INVALID, "not a tensor-core flat index");
-    TcFlatState &S = *tcs(ix);
-    if (S.n == 0) return fail(GN_ERR_EMPTY, "index is empty");
+    GN_TRY(tcflat_check(ix, k));
     if (nq < 0 || (nq > 0 && (!queries || !out_idx || !out_dist))) return fail(GN_ERR_INVALID, "bad arguments");
     if (nq == 0) return GN_OK;
+    TcFlatState &S = *tcs(ix);
     cudaStream_t st = ix->stream;
-    {
-        std::lock_guard<std::mutex> lk(ix->mu);
-        GN_TRY(upload_rows(S.q32, queries, nq, S.d * 4, S.dp / 4, st));
-        GN_TRY(S.out_idx.ensure((size_t)nq * k * 8));
-        GN_TRY(S.out_dist.ensure((size_t)nq * k * 4));
-    }
-    GN_TRY(gn_tcflat_search_knn_device(ix, S.q32.as<float>(), nq, k, S.out_idx.as<int64_t>(), S.out_dist.as<float>(),
-                                       st));
-    GN_CUDA_TRY(cudaMemcpyAsync(out_idx, S.out_idx.p, (size_t)nq * k * 8, cudaMemcpyDeviceToHost, st));
-    GN_CUDA_TRY(cudaMemcpyAsync(out_dist, S.out_dist.p, (size_t)nq * k * 4, cudaMemcpyDeviceToHost, st));
+    // the lock covers the whole call: the query, result and staging buffers are the index's
+    std::lock_guard<std::mutex> lk(ix->mu);
+    begin_blocking(ix);
+    GN_TRY(upload_queries(ix, S.q32, queries, nq, S.d * 4, S.dp / 4, st));
+    GN_TRY(S.out_idx.ensure((size_t)nq * k * 8));
+    GN_TRY(S.out_dist.ensure((size_t)nq * k * 4));
+    GN_TRY(tcflat_search_locked(ix, S.q32.as<float>(), nq, k, S.out_idx.as<int64_t>(), S.out_dist.as<float>(), st));
+    GN_TRY(download_result(ix, out_idx, S.out_idx.p, (size_t)nq * k * 8, st));
+    GN_TRY(download_result(ix, out_dist, S.out_dist.p, (size_t)nq * k * 4, st));
     return finish_blocking(ix, S.err.as<int>(), st, "tensor-core scan: a pipeline wait timed out");
 }
 
