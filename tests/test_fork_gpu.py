@@ -112,3 +112,32 @@ def test_fork_inherits_the_prober(gn):
     f = ix.fork()
     _same(f.search_knn_arrays(q, 10), ref)
     np.testing.assert_array_equal(f.last_lists_probed(len(q)), ix.last_lists_probed(len(q)))
+
+
+@pytest.mark.parametrize("kind", ["flat", "ivf", "ivf_graphs", "tc"])
+def test_threads_sharing_one_index(gn, kind):
+    """Blocking host-buffer searches from several threads on ONE index: each
+    call holds the index's lock for its whole length (its query, result and
+    pinned staging buffers are the index's), so every thread gets exactly the
+    results of the same search made alone.  Batch sizes mix small pageable
+    copies (staged through pinned memory) and larger ones (copied directly)."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    db, q = _data(60_000, 64, 3000, 3)
+    if kind == "flat":
+        ix = gn.FlatL2Index()
+    elif kind == "tc":
+        ix = gn.FlatL2TCIndex(shortlist=40)
+    else:
+        ix = gn.IVFFlatL2Index(n_clusters=128, n_probe=8, engine="tc")
+    ix.set(db)
+    if kind == "ivf_graphs":
+        ix.enable_graphs(2048, 10)
+    sizes = [1, 2, 9, 130, 2048, 1, 17, 600, 4, 1]
+    offs = np.concatenate([[0], np.cumsum(sizes)])
+    jobs = [(o, n) for o, n in zip(offs[:-1], sizes)] * 3
+    ref = {(o, n): ix.search_knn_arrays(q[o:o + n], 10) for o, n in zip(offs[:-1], sizes)}
+    with ThreadPoolExecutor(4) as pool:
+        got = list(pool.map(lambda j: (j, ix.search_knn_arrays(q[j[0]:j[0] + j[1]], 10)), jobs))
+    for j, r in got:
+        _same(r, ref[j])
